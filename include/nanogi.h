@@ -1,0 +1,184 @@
+/*
+ * nanogi-gb300 C ABI: the single host<->device boundary of the GB300 path tracer.
+ *
+ * The reference (lighttransport/nanogi) has no plugin or FFI layer. Its renderer
+ * interface is (i) the command line, (ii) the YAML scene schema and (iii) the film
+ * file, with the C++ entry points listed next to each function below. This header
+ * exposes exactly those entry points as plain C: opaque handles, plain pointers and
+ * sizes, integer status codes, and no exceptions or C++/torch types crossing it.
+ *
+ * Conventions shared by every function:
+ *   - Every call returns an ngi_status; NGI_OK is 0. On failure a human-readable
+ *     message is available from ngi_last_error() (thread-local, valid until the next
+ *     call on the same thread).
+ *   - Films are W*H*3 doubles, row 0 = the BOTTOM scanline, pixel index = y*W + x,
+ *     exactly the layout of std::vector<glm::dvec3> film in the reference
+ *     (src/nanogi.cpp:429-437, include/nanogi/rt.hpp:135-140).
+ *   - A scene handle owns its host copy, its device buffers, its CUDA stream and its
+ *     wave buffers. A handle must not be used from two host threads at once.
+ */
+#ifndef NANOGI_GB300_H
+#define NANOGI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define NGI_API __declspec(dllexport)
+#else
+#define NGI_API __attribute__((visibility("default")))
+#endif
+
+#define NGI_ABI_VERSION 1
+
+typedef enum ngi_status {
+    NGI_OK = 0,
+    NGI_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
+    NGI_ERR_IO = 2,               /* file missing / unreadable / unwritable */
+    NGI_ERR_PARSE = 3,            /* malformed YAML or OBJ, schema violation */
+    NGI_ERR_CUDA = 4,             /* CUDA runtime error (message carries the CUDA string) */
+    NGI_ERR_OUT_OF_MEMORY = 5,    /* host or device allocation failed */
+    NGI_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up */
+    NGI_ERR_UNSUPPORTED = 7,      /* valid input the reference rejects or crashes on */
+    NGI_ERR_NO_DEVICE = 8         /* no CUDA device visible */
+} ngi_status;
+
+/* Renderer names of the reference (src/nanogi.cpp:51-69); only the path tracers are built. */
+typedef enum ngi_renderer_type {
+    NGI_RENDERER_PT = 0,       /* "pt"       : ProcessSample_PT       src/nanogi.cpp:446-607 */
+    NGI_RENDERER_PTDIRECT = 1  /* "ptdirect" : ProcessSample_PTDirect src/nanogi.cpp:609-802 */
+} ngi_renderer_type;
+
+/* Arithmetic of the shading stage. Traversal is FP32 and accumulation FP64 in both. */
+typedef enum ngi_precision {
+    NGI_PRECISION_FP32 = 0,   /* tuned path: FP32 shading, FP64 film */
+    NGI_PRECISION_FP64 = 1    /* plain path: FP64 shading and path state, FP64 film */
+} ngi_precision;
+
+/* Sample -> raster mapping. The reference draws every sample uniformly over the whole
+ * image (include/nanogi/rt.hpp:733-739 with u from src/nanogi.cpp:495); STRATIFIED gives
+ * each pixel an equal share of whole passes (same expectation, lower variance). */
+typedef enum ngi_raster_mode {
+    NGI_RASTER_STRATIFIED = 0,
+    NGI_RASTER_UNIFORM = 1
+} ngi_raster_mode;
+
+/* Renderer parameters: the reference's Renderer::Params (src/nanogi.cpp:85-97) plus the
+ * replay seed and the GPU-only knobs. */
+typedef struct ngi_render_params {
+    int32_t renderer;          /* ngi_renderer_type */
+    int32_t max_num_vertices;  /* -m; -1 = unbounded (src/nanogi.cpp:2007) */
+    int64_t num_samples;       /* -n; TOTAL samples over the image (src/nanogi.cpp:2006) */
+    int32_t width;             /* -w */
+    int32_t height;            /* -h */
+    uint64_t seed;             /* Philox key: (seed, sample index) makes every path replayable */
+    int64_t sample_offset;     /* first global sample index (sharded / resumed renders) */
+    int32_t precision;         /* ngi_precision */
+    int32_t raster_mode;       /* ngi_raster_mode */
+    int32_t wave_size;         /* path slots resident on the device; 0 = auto */
+    int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
+} ngi_render_params;
+
+/* Counters of the last render on a scene handle (per-stage ray counts etc). */
+typedef struct ngi_render_stats {
+    int64_t camera_rays;       /* paths started (= samples processed) */
+    int64_t extension_rays;    /* closest-hit rays traced (camera rays included) */
+    int64_t shadow_rays;       /* visibility rays traced (NEE) */
+    int64_t film_contributions;/* non-zero contributions added to the film */
+    int64_t iterations;        /* wave iterations executed */
+    int64_t nonfinite;         /* NaN/Inf contributions dropped (reported, never trapped) */
+    double render_ms;          /* device time of the render (CUDA events on the scene stream) */
+} ngi_render_stats;
+
+/* Scene summary (host side; available without a GPU). */
+typedef struct ngi_scene_info {
+    int32_t num_primitives;
+    int32_t num_lights;
+    int32_t sensor_index;      /* index of the E primitive, -1 if none */
+    int32_t sensor_type;       /* 0 = area, 1 = pinhole (EType, rt.hpp:360-364) */
+    int64_t num_triangles;
+    int64_t num_vertices;
+    double bound_min[3];
+    double bound_max[3];
+    int32_t device_ready;      /* 1 once the BVH has been built on the device */
+    int32_t bvh_nodes;         /* compressed 8-wide nodes */
+    int64_t bvh_bytes;         /* node + triangle bytes resident in HBM */
+    double bvh_build_ms;       /* device time of the last BVH build */
+} ngi_scene_info;
+
+typedef struct ngi_scene ngi_scene;
+
+/* ---- errors / version ---------------------------------------------------------- */
+
+/* Message of the last failed call on this thread ("" if none). */
+NGI_API const char* ngi_last_error(void);
+NGI_API int32_t ngi_abi_version(void);
+
+/* ---- scene ------------------------------------------------------------------------ */
+
+/* Scene::Load(const std::string& path, double aspect)  include/nanogi/rt.hpp:1519-2154.
+ * Parses the YAML scene (schema versions 3..5, schema.yml:33-334) and its OBJ meshes,
+ * flattens them into host SoA arrays. Does not touch the GPU. */
+NGI_API ngi_status ngi_scene_load(const char* yaml_path, double aspect, ngi_scene** out_scene);
+
+/* Scene::~Scene  include/nanogi/rt.hpp:1509-1513. Frees host and device memory. */
+NGI_API void ngi_scene_free(ngi_scene* scene);
+
+NGI_API ngi_status ngi_scene_get_info(const ngi_scene* scene, ngi_scene_info* out_info);
+
+/* Uploads the flattened scene and builds the compressed 8-wide BVH on the GPU: the
+ * counterpart of the Embree build in include/nanogi/rt.hpp:2087-2143. Called implicitly
+ * by the first render/intersect; explicit so its cost can be measured apart. */
+NGI_API ngi_status ngi_scene_build(ngi_scene* scene);
+
+/* ---- rendering --------------------------------------------------------------------- */
+
+/* Renderer::Render(const Scene&, std::vector<glm::dvec3>& film)  src/nanogi.cpp:182-221
+ * with RenderProcess's gather and W*H/N normalisation (src/nanogi.cpp:429-437).
+ * film_rgb: HOST array of width*height*3 doubles, overwritten with the normalised film. */
+NGI_API ngi_status ngi_render(ngi_scene* scene, const ngi_render_params* params, double* film_rgb);
+
+/* Same render, film left on the device: d_film_rgb is a DEVICE pointer to width*height*3
+ * doubles which receives the RAW (un-normalised) sums added to its current contents; the
+ * caller scales by width*height/num_samples. stream: cudaStream_t or NULL for the scene's
+ * own stream. Returns after the work is enqueued AND complete. */
+NGI_API ngi_status ngi_render_device(ngi_scene* scene, const ngi_render_params* params,
+                                     double* d_film_rgb, void* stream);
+
+NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats* out_stats);
+
+/* ---- parity hooks ------------------------------------------------------------------ */
+
+/* Scene::Intersect(ray, isect, minT, maxT)  include/nanogi/rt.hpp:2162-2244, restricted
+ * to what the Embree query returns: nearest triangle, t and barycentric u, v.
+ * rays: HOST array of n*8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax).
+ * prim_out[i] = global triangle index (primitives in YAML order, faces in mesh order)
+ * or -1 on a miss; t_out[i]; uv_out[2i..2i+1] = (u, v) with hit point
+ * (1-u-v)*p0 + u*p1 + v*p2 (Embree convention, rt.hpp:2212). Any output may be NULL. */
+NGI_API ngi_status ngi_intersect(ngi_scene* scene, const float* rays, int64_t n,
+                                 int32_t* prim_out, float* t_out, float* uv_out);
+
+/* Scene::Visible(p1, p2)  include/nanogi/rt.hpp:2251-2261 for n point pairs.
+ * points: HOST array of n*6 doubles (p1.xyz, p2.xyz). visible_out[i] = 1 if unoccluded. */
+NGI_API ngi_status ngi_visible(ngi_scene* scene, const double* points, int64_t n,
+                               uint8_t* visible_out);
+
+/* ---- film I/O ------------------------------------------------------------------------ */
+
+/* SaveImage(path, film, w, h)  include/nanogi/basic.hpp:506-672 for ".hdr" (Radiance
+ * RGBE, upright image: the bottom film row is written last) and ".pfm". */
+NGI_API ngi_status ngi_save_image(const char* path, const double* film_rgb, int32_t width, int32_t height);
+
+/* Reads back a ".hdr" written by ngi_save_image into width*height*3 doubles, row 0 =
+ * bottom (test helper; no reference counterpart beyond Texture::Load of .hdr, rt.hpp:168). */
+NGI_API ngi_status ngi_load_hdr(const char* path, double* film_rgb, int32_t width, int32_t height);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NANOGI_GB300_H */

@@ -1,0 +1,550 @@
+// GPU construction of the compressed 8-wide BVH.
+//
+// Replaces the Embree build of include/nanogi/rt.hpp:2087-2143. Pipeline (all on device):
+//   1. per-triangle bounds and centroid bounds
+//   2. 63-bit Morton codes of the centroids, radix sort (CUB)
+//   3. binary radix tree (Karras, HPG 2012), one thread per internal node
+//   4. bottom-up bounds refit with per-node arrival counters
+//   5. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017):
+//      each node greedily opens its largest-area internal child until it has 8 children,
+//      subtrees of <= 3 triangles become leaves, children are assigned to slots by ray
+//      octant, and child boxes are quantised to 8 bits per plane relative to the parent.
+//   6. triangles, normals and uvs are gathered into leaf order.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "device_scene.hpp"
+#include "ngi_device.cuh"
+
+namespace ngi {
+
+namespace {
+
+constexpr int kLeafMax = 3;   // triangles per leaf child (unary count field holds 1..3)
+constexpr uint32_t kLeafFlag = 0x80000000u;
+
+#define BVH_CHECK(x)                                                                          \
+    do {                                                                                      \
+        cudaError_t e_ = (x);                                                                 \
+        if (e_ != cudaSuccess)                                                                \
+            throw DeviceError(std::string("CUDA error in BVH build: ") + cudaGetErrorString(e_) \
+                              + " at " #x);                                                   \
+    } while (0)
+
+__device__ __forceinline__ int float_to_ordered(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__host__ __device__ __forceinline__ float ordered_to_float(int i) {
+    int b = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+__global__ void k_tri_bounds(const float* __restrict__ pos, int n, float4* __restrict__ lo,
+                             float4* __restrict__ hi, int* __restrict__ cbounds) {
+    __shared__ int smin[3][32], smax[3][32];
+    int cmin[3] = {INT_MAX, INT_MAX, INT_MAX}, cmax[3] = {INT_MIN, INT_MIN, INT_MIN};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* p = pos + 9 * (size_t)i;
+        float l[3], h[3];
+        for (int k = 0; k < 3; k++) {
+            l[k] = fminf(fminf(p[k], p[3 + k]), p[6 + k]);
+            h[k] = fmaxf(fmaxf(p[k], p[3 + k]), p[6 + k]);
+        }
+        lo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+        hi[i] = make_float4(h[0], h[1], h[2], 0.0f);
+        for (int k = 0; k < 3; k++) {
+            const int c = float_to_ordered(0.5f * (l[k] + h[k]));
+            cmin[k] = min(cmin[k], c);
+            cmax[k] = max(cmax[k], c);
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            cmin[k] = min(cmin[k], __shfl_xor_sync(0xFFFFFFFFu, cmin[k], o));
+            cmax[k] = max(cmax[k], __shfl_xor_sync(0xFFFFFFFFu, cmax[k], o));
+        }
+        if (lane == 0) { smin[k][warp] = cmin[k]; smax[k][warp] = cmax[k]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        int a = INT_MAX, b = INT_MIN;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a = min(a, smin[k][w]); b = max(b, smax[k][w]); }
+        atomicMin(&cbounds[k], a);
+        atomicMax(&cbounds[3 + k], b);
+    }
+}
+
+__device__ __forceinline__ uint64_t expand_bits21(uint64_t x) {
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, int n,
+                         const int* __restrict__ cbounds, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 l = lo[i], h = hi[i];
+    const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
+    uint64_t q[3];
+    for (int k = 0; k < 3; k++) {
+        const float mn = ordered_to_float(cbounds[k]), mx = ordered_to_float(cbounds[3 + k]);
+        const float ext = mx - mn;
+        float f = ext > 0.0f ? (c[k] - mn) / ext : 0.0f;
+        f = fminf(fmaxf(f, 0.0f), 1.0f);
+        q[k] = (uint64_t)fminf(f * 2097152.0f, 2097151.0f);
+    }
+    keys[i] = (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
+    vals[i] = (uint32_t)i;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clzll(a ^ b);
+}
+
+// Karras 2012: internal node i covers sorted range [first, last], split after gamma.
+__global__ void k_radix_tree(const uint64_t* __restrict__ keys, int n, uint32_t* __restrict__ left,
+                             uint32_t* __restrict__ right, int* __restrict__ int_parent,
+                             int* __restrict__ leaf_parent, int2* __restrict__ range) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int64_t lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for (int64_t t = lmax / 2; t >= 1; t /= 2)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int64_t j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int64_t s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+    const int64_t first = d > 0 ? i : j, last = d > 0 ? j : i;
+    uint32_t lref, rref;
+    if (first == gamma) { lref = kLeafFlag | (uint32_t)gamma; leaf_parent[gamma] = (int)i; }
+    else { lref = (uint32_t)gamma; int_parent[gamma] = (int)i; }
+    if (last == gamma + 1) { rref = kLeafFlag | (uint32_t)(gamma + 1); leaf_parent[gamma + 1] = (int)i; }
+    else { rref = (uint32_t)(gamma + 1); int_parent[gamma + 1] = (int)i; }
+    left[i] = lref;
+    right[i] = rref;
+    range[i] = make_int2((int)first, (int)last);
+    if (i == 0) int_parent[0] = -1;
+}
+
+__device__ __forceinline__ float4 ld_cg(const float4* p) { return __ldcg(p); }
+
+// Bottom-up bounds: the second thread to reach a node computes it.
+__global__ void k_refit(int n, const uint32_t* __restrict__ sorted_tri, const float4* __restrict__ tlo,
+                        const float4* __restrict__ thi, const uint32_t* __restrict__ left,
+                        const uint32_t* __restrict__ right, const int* __restrict__ int_parent,
+                        const int* __restrict__ leaf_parent, float4* leaf_lo, float4* leaf_hi, float4* int_lo,
+                        float4* int_hi, int* __restrict__ arrivals, int* __restrict__ error_flag) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t tri = sorted_tri[j];
+    leaf_lo[j] = tlo[tri];
+    leaf_hi[j] = thi[tri];
+    __threadfence();
+    int p = leaf_parent[j];
+    // A radix tree over 63-bit keys with 32-bit index tie-breaks is at most ~96 levels deep.
+    for (int steps = 0; p >= 0; steps++) {
+        if (steps > 256) { atomicOr(error_flag, 1); return; }
+        if (atomicAdd(&arrivals[p], 1) == 0) return;
+        __threadfence();
+        const uint32_t l = left[p], r = right[p];
+        const float4 a_lo = (l & kLeafFlag) ? ld_cg(&leaf_lo[l & ~kLeafFlag]) : ld_cg(&int_lo[l]);
+        const float4 a_hi = (l & kLeafFlag) ? ld_cg(&leaf_hi[l & ~kLeafFlag]) : ld_cg(&int_hi[l]);
+        const float4 b_lo = (r & kLeafFlag) ? ld_cg(&leaf_lo[r & ~kLeafFlag]) : ld_cg(&int_lo[r]);
+        const float4 b_hi = (r & kLeafFlag) ? ld_cg(&leaf_hi[r & ~kLeafFlag]) : ld_cg(&int_hi[r]);
+        __stcg(&int_lo[p], make_float4(fminf(a_lo.x, b_lo.x), fminf(a_lo.y, b_lo.y), fminf(a_lo.z, b_lo.z), 0.0f));
+        __stcg(&int_hi[p], make_float4(fmaxf(a_hi.x, b_hi.x), fmaxf(a_hi.y, b_hi.y), fmaxf(a_hi.z, b_hi.z), 0.0f));
+        __threadfence();
+        p = int_parent[p];
+    }
+}
+
+struct BinView {
+    const uint32_t* left;
+    const uint32_t* right;
+    const int2* range;
+    const float4* leaf_lo;
+    const float4* leaf_hi;
+    const float4* int_lo;
+    const float4* int_hi;
+};
+
+__device__ __forceinline__ int ref_count(const BinView& b, uint32_t ref) {
+    if (ref & kLeafFlag) return 1;
+    const int2 r = b.range[ref];
+    return r.y - r.x + 1;
+}
+__device__ __forceinline__ void ref_bounds(const BinView& b, uint32_t ref, float4& lo, float4& hi) {
+    if (ref & kLeafFlag) { lo = b.leaf_lo[ref & ~kLeafFlag]; hi = b.leaf_hi[ref & ~kLeafFlag]; }
+    else { lo = b.int_lo[ref]; hi = b.int_hi[ref]; }
+}
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    const float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
+    return x * y + y * z + z * x;
+}
+__device__ __forceinline__ int ref_first(const BinView& b, uint32_t ref) {
+    return (ref & kLeafFlag) ? (int)(ref & ~kLeafFlag) : b.range[ref].x;
+}
+
+struct WorkItem {
+    uint32_t ref;   // binary node (or leaf, for a 1-triangle scene) to expand
+    uint32_t node;  // output 8-wide node index
+};
+
+// Plan: choose the (up to) 8 children of each new node, count internal children and leaf triangles.
+__global__ void k_collapse_plan(BinView b, const WorkItem* __restrict__ work, int nwork,
+                                uint32_t* __restrict__ children, int* __restrict__ n_int, int* __restrict__ n_tri) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwork) return;
+    const uint32_t ref = work[w].ref;
+    uint32_t ch[8];
+    int nc = 0;
+    if (ref & kLeafFlag) {
+        ch[nc++] = ref;
+    } else {
+        ch[nc++] = b.left[ref];
+        ch[nc++] = b.right[ref];
+        while (nc < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int c = 0; c < nc; c++) {
+                if ((ch[c] & kLeafFlag) || ref_count(b, ch[c]) <= kLeafMax) continue;
+                float4 lo, hi;
+                ref_bounds(b, ch[c], lo, hi);
+                const float a = half_area(lo, hi);
+                if (a > best_area) { best_area = a; best = c; }
+            }
+            if (best < 0) break;
+            const uint32_t open = ch[best];
+            ch[best] = b.left[open];
+            ch[nc++] = b.right[open];
+        }
+    }
+    int ni = 0, nt = 0;
+    for (int c = 0; c < 8; c++) {
+        uint32_t r = c < nc ? ch[c] : 0xFFFFFFFFu;
+        children[8 * (size_t)w + c] = r;
+        if (c < nc) {
+            const int cnt = ref_count(b, r);
+            if (!(r & kLeafFlag) && cnt > kLeafMax) ni++;
+            else nt += cnt;
+        }
+    }
+    n_int[w] = ni;
+    n_tri[w] = nt;
+}
+
+// Emit: quantise, assign slots, write the node, gather leaf triangles, queue internal children.
+__global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, int nwork,
+                                const uint32_t* __restrict__ children, const int* __restrict__ int_off,
+                                const int* __restrict__ tri_off, uint32_t node_base, uint32_t tri_base_all,
+                                const uint32_t* __restrict__ sorted_tri, const float* __restrict__ pos,
+                                CwNode* __restrict__ nodes, float4* __restrict__ tris_out,
+                                uint32_t* __restrict__ perm, WorkItem* __restrict__ next_work) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwork) return;
+    uint32_t ch[8];
+    int nc = 0;
+    for (int c = 0; c < 8; c++) {
+        const uint32_t r = children[8 * (size_t)w + c];
+        if (r != 0xFFFFFFFFu) ch[nc++] = r;
+    }
+    float4 clo[8], chi[8];
+    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+    for (int c = 0; c < nc; c++) {
+        ref_bounds(b, ch[c], clo[c], chi[c]);
+        lo.x = fminf(lo.x, clo[c].x); lo.y = fminf(lo.y, clo[c].y); lo.z = fminf(lo.z, clo[c].z);
+        hi.x = fmaxf(hi.x, chi[c].x); hi.y = fmaxf(hi.y, chi[c].y); hi.z = fmaxf(hi.z, chi[c].z);
+    }
+    CwNode node;
+    node.px = lo.x; node.py = lo.y; node.pz = lo.z;
+    uint32_t ebits[3];
+    float inv_scale[3];
+    const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
+    for (int k = 0; k < 3; k++) {
+        const float ext = __fsub_ru(h3[k], l3[k]);
+        const float s = __fdiv_ru(ext, 255.0f);
+        uint32_t bits = __float_as_uint(s);
+        uint32_t e = (bits >> 23) & 0xFFu;
+        if (bits & 0x7FFFFFu) e += 1;
+        if (e < 1) e = 1;
+        if (e > 253) e = 253;
+        ebits[k] = e;
+        inv_scale[k] = __uint_as_float((254u - e) << 23);
+    }
+    node.ex = (uint8_t)ebits[0]; node.ey = (uint8_t)ebits[1]; node.ez = (uint8_t)ebits[2];
+
+    // Octant slot assignment: slot s holds the child a ray of octant s should visit first.
+    const float ncx = 0.5f * (lo.x + hi.x), ncy = 0.5f * (lo.y + hi.y), ncz = 0.5f * (lo.z + hi.z);
+    float cost[8][8];
+    for (int c = 0; c < nc; c++) {
+        const float dx = 0.5f * (clo[c].x + chi[c].x) - ncx;
+        const float dy = 0.5f * (clo[c].y + chi[c].y) - ncy;
+        const float dz = 0.5f * (clo[c].z + chi[c].z) - ncz;
+        for (int s = 0; s < 8; s++)
+            cost[c][s] = ((s & 1) ? -dx : dx) + ((s & 2) ? -dy : dy) + ((s & 4) ? -dz : dz);
+    }
+    int slot_of[8];
+    uint32_t slot_used = 0, child_done = 0;
+    for (int it = 0; it < nc; it++) {
+        float best = INFINITY;
+        int bc = -1, bs = -1;
+        for (int c = 0; c < nc; c++) {
+            if (child_done & (1u << c)) continue;
+            for (int s = 0; s < 8; s++) {
+                if (slot_used & (1u << s)) continue;
+                if (cost[c][s] < best || bc < 0) { best = cost[c][s]; bc = c; bs = s; }
+            }
+        }
+        slot_of[bc] = bs;
+        child_done |= 1u << bc;
+        slot_used |= 1u << bs;
+    }
+    int child_in_slot[8];
+    for (int s = 0; s < 8; s++) child_in_slot[s] = -1;
+    for (int c = 0; c < nc; c++) child_in_slot[slot_of[c]] = c;
+
+    const uint32_t child_base = node_base + (uint32_t)int_off[w];
+    const uint32_t tri_base = tri_base_all + (uint32_t)tri_off[w];
+    node.child_base = child_base;
+    node.tri_base = tri_base;
+    uint32_t imask = 0;
+    int int_rank = 0, tri_rank = 0;
+    for (int s = 0; s < 8; s++) {
+        const int c = child_in_slot[s];
+        if (c < 0) {
+            node.meta[s] = 0;
+            node.qlo_x[s] = node.qlo_y[s] = node.qlo_z[s] = 0;
+            node.qhi_x[s] = node.qhi_y[s] = node.qhi_z[s] = 0;
+            continue;
+        }
+        const float cl[3] = {clo[c].x, clo[c].y, clo[c].z}, chh[3] = {chi[c].x, chi[c].y, chi[c].z};
+        uint8_t ql[3], qh[3];
+        for (int k = 0; k < 3; k++) {
+            const float a = floorf(__fsub_rd(cl[k], l3[k]) * inv_scale[k]);
+            const float bq = ceilf(__fsub_ru(chh[k], l3[k]) * inv_scale[k]);
+            ql[k] = (uint8_t)fminf(fmaxf(a, 0.0f), 255.0f);
+            qh[k] = (uint8_t)fminf(fmaxf(bq, 0.0f), 255.0f);
+        }
+        node.qlo_x[s] = ql[0]; node.qlo_y[s] = ql[1]; node.qlo_z[s] = ql[2];
+        node.qhi_x[s] = qh[0]; node.qhi_y[s] = qh[1]; node.qhi_z[s] = qh[2];
+        const uint32_t r = ch[c];
+        const int cnt = ref_count(b, r);
+        if (!(r & kLeafFlag) && cnt > kLeafMax) {
+            imask |= 1u << s;
+            node.meta[s] = (uint8_t)(0x20u | (24u + (uint32_t)s));
+            next_work[int_off[w] + int_rank] = WorkItem{r, child_base + (uint32_t)int_rank};
+            int_rank++;
+        } else {
+            const uint32_t unary = cnt == 1 ? 1u : (cnt == 2 ? 3u : 7u);
+            node.meta[s] = (uint8_t)((unary << 5) | (uint32_t)tri_rank);
+            const int first = ref_first(b, r);
+            for (int q = 0; q < cnt; q++) {
+                const uint32_t tri = sorted_tri[first + q];
+                const uint32_t dst = tri_base + (uint32_t)tri_rank + (uint32_t)q;
+                const float* p = pos + 9 * (size_t)tri;
+                tris_out[3 * (size_t)dst + 0] = make_float4(p[0], p[1], p[2], __uint_as_float(tri));
+                tris_out[3 * (size_t)dst + 1] = make_float4(p[3], p[4], p[5], 0.0f);
+                tris_out[3 * (size_t)dst + 2] = make_float4(p[6], p[7], p[8], 0.0f);
+                perm[dst] = tri;
+            }
+            tri_rank += cnt;
+        }
+    }
+    node.imask = (uint8_t)imask;
+    nodes[work[w].node] = node;
+}
+
+__global__ void k_gather_shading(int n, const uint32_t* __restrict__ perm, const float* __restrict__ nrm,
+                                 const float* __restrict__ uv, const int* __restrict__ tri_prim,
+                                 float4* __restrict__ nrm_out, float2* __restrict__ uv_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t t = perm[i];
+    const float* q = nrm + 9 * (size_t)t;
+    nrm_out[3 * (size_t)i + 0] = make_float4(q[0], q[1], q[2], __int_as_float(tri_prim[t]));
+    nrm_out[3 * (size_t)i + 1] = make_float4(q[3], q[4], q[5], 0.0f);
+    nrm_out[3 * (size_t)i + 2] = make_float4(q[6], q[7], q[8], 0.0f);
+    const float* u = uv + 6 * (size_t)t;
+    uv_out[3 * (size_t)i + 0] = make_float2(u[0], u[1]);
+    uv_out[3 * (size_t)i + 1] = make_float2(u[2], u[3]);
+    uv_out[3 * (size_t)i + 2] = make_float2(u[4], u[5]);
+}
+
+template <typename T>
+T* dev_alloc(size_t count, std::vector<void*>& temps) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    BVH_CHECK(cudaMalloc(&p, count * sizeof(T)));
+    temps.push_back(p);
+    return (T*)p;
+}
+
+}  // namespace
+
+// Builds the BVH of the n triangles in d_pos (9 floats each, original order).
+void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const float* d_uv, const int* d_tri_prim,
+              int n, cudaStream_t stream) {
+    std::vector<void*> temps;
+    auto free_temps = [&]() {
+        for (void* p : temps) cudaFree(p);
+        temps.clear();
+    };
+    try {
+        cudaEvent_t e0, e1;
+        BVH_CHECK(cudaEventCreate(&e0));
+        BVH_CHECK(cudaEventCreate(&e1));
+        BVH_CHECK(cudaEventRecord(e0, stream));
+        ds.num_nodes = 0;
+        ds.bvh_depth = 0;
+        if (n > 0) {
+            const int T = 256;
+            const int nb = (n + T - 1) / T;
+            float4* tlo = dev_alloc<float4>(n, temps);
+            float4* thi = dev_alloc<float4>(n, temps);
+            int* cb = dev_alloc<int>(6, temps);
+            const int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+            BVH_CHECK(cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+            k_tri_bounds<<<std::min(nb, 152 * 8), T, 0, stream>>>(d_pos, n, tlo, thi, cb);
+            uint64_t* keys = dev_alloc<uint64_t>(n, temps);
+            uint64_t* keys_s = dev_alloc<uint64_t>(n, temps);
+            uint32_t* vals = dev_alloc<uint32_t>(n, temps);
+            uint32_t* vals_s = dev_alloc<uint32_t>(n, temps);
+            k_morton<<<nb, T, 0, stream>>>(tlo, thi, n, cb, keys, vals);
+            size_t tmp_bytes = 0;
+            BVH_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_s, vals, vals_s, n, 0, 63, stream));
+            void* tmp = dev_alloc<uint8_t>(tmp_bytes, temps);
+            BVH_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_s, vals, vals_s, n, 0, 63, stream));
+
+            const int ni = std::max(n - 1, 1);
+            uint32_t* left = dev_alloc<uint32_t>(ni, temps);
+            uint32_t* right = dev_alloc<uint32_t>(ni, temps);
+            int* int_parent = dev_alloc<int>(ni, temps);
+            int* leaf_parent = dev_alloc<int>(n, temps);
+            int2* range = dev_alloc<int2>(ni, temps);
+            float4* leaf_lo = dev_alloc<float4>(n, temps);
+            float4* leaf_hi = dev_alloc<float4>(n, temps);
+            float4* int_lo = dev_alloc<float4>(ni, temps);
+            float4* int_hi = dev_alloc<float4>(ni, temps);
+            int* arrivals = dev_alloc<int>(ni + 1, temps);  // last entry: error flag
+            BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));
+            if (n == 1) {
+                BVH_CHECK(cudaMemsetAsync(leaf_parent, 0xFF, sizeof(int), stream));  // -1
+            } else {
+                k_radix_tree<<<(n - 1 + T - 1) / T, T, 0, stream>>>(keys_s, n, left, right, int_parent, leaf_parent, range);
+            }
+            k_refit<<<nb, T, 0, stream>>>(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, leaf_lo, leaf_hi,
+                                         int_lo, int_hi, arrivals, arrivals + ni);
+            BVH_CHECK(cudaGetLastError());
+            int refit_err = 0;
+            BVH_CHECK(cudaMemcpyAsync(&refit_err, arrivals + ni, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            if (refit_err) throw DeviceError("BVH refit walked past the maximum tree depth");
+
+            // 8-wide collapse, one level per iteration.
+            const size_t max_nodes = (size_t)ni + 1;
+            CwNode* nodes = nullptr;
+            BVH_CHECK(cudaMalloc(&nodes, max_nodes * sizeof(CwNode)));
+            temps.push_back(nodes);
+            float4* tris_out = nullptr;
+            BVH_CHECK(cudaMalloc(&tris_out, 3 * (size_t)n * sizeof(float4)));
+            uint32_t* perm = dev_alloc<uint32_t>(n, temps);
+            WorkItem* work_a = dev_alloc<WorkItem>(max_nodes, temps);
+            WorkItem* work_b = dev_alloc<WorkItem>(max_nodes, temps);
+            uint32_t* children = dev_alloc<uint32_t>(8 * max_nodes, temps);
+            int* n_int = dev_alloc<int>(max_nodes + 1, temps);
+            int* n_tri = dev_alloc<int>(max_nodes + 1, temps);
+            int* int_off = dev_alloc<int>(max_nodes + 1, temps);
+            int* tri_off = dev_alloc<int>(max_nodes + 1, temps);
+            size_t scan_bytes = 0;
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, n_int, int_off, (int)max_nodes + 1, stream));
+            void* scan_tmp = dev_alloc<uint8_t>(scan_bytes, temps);
+
+            const WorkItem root{n == 1 ? (kLeafFlag | 0u) : 0u, 0u};
+            BVH_CHECK(cudaMemcpyAsync(work_a, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
+            BinView bv{left, right, range, leaf_lo, leaf_hi, int_lo, int_hi};
+            uint32_t node_count = 1, tri_count = 0;
+            int nwork = 1, depth = 0;
+            while (nwork > 0) {
+                depth++;
+                const int gb = (nwork + 127) / 128;
+                k_collapse_plan<<<gb, 128, 0, stream>>>(bv, work_a, nwork, children, n_int, n_tri);
+                BVH_CHECK(cudaMemsetAsync(n_int + nwork, 0, sizeof(int), stream));
+                BVH_CHECK(cudaMemsetAsync(n_tri + nwork, 0, sizeof(int), stream));
+                BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_int, int_off, nwork + 1, stream));
+                BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_tri, tri_off, nwork + 1, stream));
+                k_collapse_emit<<<gb, 128, 0, stream>>>(bv, work_a, nwork, children, int_off, tri_off, node_count,
+                                                       tri_count, vals_s, d_pos, nodes, tris_out, perm, work_b);
+                BVH_CHECK(cudaGetLastError());
+                int totals[2];
+                BVH_CHECK(cudaMemcpyAsync(&totals[0], int_off + nwork, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                BVH_CHECK(cudaMemcpyAsync(&totals[1], tri_off + nwork, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                BVH_CHECK(cudaStreamSynchronize(stream));
+                node_count += (uint32_t)totals[0];
+                tri_count += (uint32_t)totals[1];
+                nwork = totals[0];
+                std::swap(work_a, work_b);
+                if (depth > 4096) throw DeviceError("BVH collapse did not terminate");
+            }
+            if ((int)tri_count != n) {
+                cudaFree(tris_out);
+                throw DeviceError("BVH collapse lost triangles: " + std::to_string(tri_count) + " of " + std::to_string(n));
+            }
+            // Shrink the node array to its exact size.
+            CwNode* nodes_exact = nullptr;
+            BVH_CHECK(cudaMalloc(&nodes_exact, (size_t)node_count * sizeof(CwNode)));
+            BVH_CHECK(cudaMemcpyAsync(nodes_exact, nodes, (size_t)node_count * sizeof(CwNode), cudaMemcpyDeviceToDevice, stream));
+            float4* nrm_out = nullptr;
+            float2* uv_out = nullptr;
+            BVH_CHECK(cudaMalloc(&nrm_out, 3 * (size_t)n * sizeof(float4)));
+            BVH_CHECK(cudaMalloc(&uv_out, 3 * (size_t)n * sizeof(float2)));
+            k_gather_shading<<<nb, T, 0, stream>>>(n, perm, d_nrm, d_uv, d_tri_prim, nrm_out, uv_out);
+            BVH_CHECK(cudaGetLastError());
+            ds.nodes = nodes_exact;
+            ds.tris = tris_out;
+            ds.nrm = nrm_out;
+            ds.uv = uv_out;
+            ds.num_nodes = (int)node_count;
+            ds.bvh_depth = depth;
+        }
+        BVH_CHECK(cudaEventRecord(e1, stream));
+        BVH_CHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ds.build_ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        free_temps();
+    } catch (...) {
+        cudaStreamSynchronize(stream);
+        free_temps();
+        throw;
+    }
+}
+
+}  // namespace ngi

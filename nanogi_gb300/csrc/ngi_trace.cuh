@@ -1,0 +1,204 @@
+// Ray traversal on the GPU: watertight ray/triangle test and compressed 8-wide BVH walk.
+//
+// Replaces Embree's rtcIntersect (include/nanogi/rt.hpp:2162-2189) and the closest-hit
+// visibility query of Scene::Visible (rt.hpp:2251-2261). Everything here is FP32, like
+// the reference's float RTCRay (rt.hpp:2166-2173) over float vertices (rt.hpp:2119-2121).
+//
+// The triangle test is the watertight algorithm of Woop, Benthin and Wald (JCGT 2013)
+// written with explicit round-to-nearest intrinsics, so no multiply-add is contracted and
+// the result is the same float the CPU oracle computes for the same ray and triangle.
+#pragma once
+
+#include "ngi_device.cuh"
+
+namespace ngi {
+
+struct RayPre {
+    float ox, oy, oz;
+    float Sx, Sy, Sz;
+    int kx, ky, kz;
+};
+
+NGI_D float comp3(float a, float b, float c, int k) { return k == 0 ? a : (k == 1 ? b : c); }
+
+// Per-ray shear constants (Woop et al. 2013, section 3).
+NGI_D RayPre ray_precompute(float ox, float oy, float oz, float dx, float dy, float dz) {
+    RayPre r;
+    r.ox = ox; r.oy = oy; r.oz = oz;
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    const float dkz = comp3(dx, dy, dz, kz);
+    if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = __fdiv_rn(comp3(dx, dy, dz, kx), dkz);
+    r.Sy = __fdiv_rn(comp3(dx, dy, dz, ky), dkz);
+    r.Sz = __fdiv_rn(1.0f, dkz);
+    return r;
+}
+
+// Watertight test. On a hit with tmin <= t < tbest returns true with t and the Embree
+// barycentrics (u weights p2, v weights p3).
+NGI_D bool tri_intersect(const RayPre& r, float4 p0, float4 p1, float4 p2, float tmin, float tbest,
+                         float& t_out, float& u_out, float& v_out) {
+    const float A0 = __fsub_rn(p0.x, r.ox), A1 = __fsub_rn(p0.y, r.oy), A2 = __fsub_rn(p0.z, r.oz);
+    const float B0 = __fsub_rn(p1.x, r.ox), B1 = __fsub_rn(p1.y, r.oy), B2 = __fsub_rn(p1.z, r.oz);
+    const float C0 = __fsub_rn(p2.x, r.ox), C1 = __fsub_rn(p2.y, r.oy), C2 = __fsub_rn(p2.z, r.oz);
+    const float Akx = comp3(A0, A1, A2, r.kx), Aky = comp3(A0, A1, A2, r.ky), Akz = comp3(A0, A1, A2, r.kz);
+    const float Bkx = comp3(B0, B1, B2, r.kx), Bky = comp3(B0, B1, B2, r.ky), Bkz = comp3(B0, B1, B2, r.kz);
+    const float Ckx = comp3(C0, C1, C2, r.kx), Cky = comp3(C0, C1, C2, r.ky), Ckz = comp3(C0, C1, C2, r.kz);
+    const float Ax = __fsub_rn(Akx, __fmul_rn(r.Sx, Akz));
+    const float Ay = __fsub_rn(Aky, __fmul_rn(r.Sy, Akz));
+    const float Bx = __fsub_rn(Bkx, __fmul_rn(r.Sx, Bkz));
+    const float By = __fsub_rn(Bky, __fmul_rn(r.Sy, Bkz));
+    const float Cx = __fsub_rn(Ckx, __fmul_rn(r.Sx, Ckz));
+    const float Cy = __fsub_rn(Cky, __fmul_rn(r.Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // Edge case: the products of two floats are exact in double, so one rounding.
+        U = (float)__dsub_rn((double)Cx * (double)By, (double)Cy * (double)Bx);
+        V = (float)__dsub_rn((double)Ax * (double)Cy, (double)Ay * (double)Cx);
+        W = (float)__dsub_rn((double)Bx * (double)Ay, (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __fdiv_rn(1.0f, det);
+    const float t = __fmul_rn(T, rcp);
+    if (!(t >= tmin && t < tbest)) return false;
+    t_out = t;
+    u_out = __fmul_rn(V, rcp);
+    v_out = __fmul_rn(W, rcp);
+    return true;
+}
+
+constexpr int kTraversalStack = 64;
+// Relative padding of the box interval: keeps the box test conservative against the few
+// ulps of rounding in the slab distances (Ize, JCGT 2013).
+constexpr float kBoxLo = 1.0f - 1.0f / 1048576.0f;
+constexpr float kBoxHi = 1.0f + 1.0f / 1048576.0f;
+
+struct TraceStats {
+    uint32_t nodes;
+    uint32_t tris;
+};
+
+NGI_D float byte_to_float(uint32_t word, int b) { return (float)((word >> (8 * b)) & 0xFFu); }
+
+// Intersects the 8 children of a node; returns the CWBVH hit mask
+// (bits 24..31: internal children by traversal priority, bits 0..23: leaf triangles).
+NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, float ox, float oy, float oz,
+                                  float idx_, float idy, float idz, uint32_t octinv,
+                                  float tmin, float tbest, uint32_t& child_base, uint32_t& tri_base,
+                                  uint32_t& imask) {
+    const float4* np = reinterpret_cast<const float4*>(nodes + idx);
+    const float4 n0 = __ldg(np + 0);
+    const float4 n1 = __ldg(np + 1);
+    const float4 n2 = __ldg(np + 2);
+    const float4 n3 = __ldg(np + 3);
+    const float4 n4 = __ldg(np + 4);
+    const uint32_t e = __float_as_uint(n0.w);
+    imask = e >> 24;
+    child_base = __float_as_uint(n1.x);
+    tri_base = __float_as_uint(n1.y);
+    const float sx = __uint_as_float((e & 0xFFu) << 23) * idx_;
+    const float sy = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idy;
+    const float sz = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idz;
+    const float ax = (n0.x - ox) * idx_;
+    const float ay = (n0.y - oy) * idy;
+    const float az = (n0.z - oz) * idz;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        const uint32_t meta4 = __float_as_uint(half == 0 ? n1.z : n1.w);
+        const uint32_t qlx = __float_as_uint(half == 0 ? n2.x : n2.y);
+        const uint32_t qly = __float_as_uint(half == 0 ? n2.z : n2.w);
+        const uint32_t qlz = __float_as_uint(half == 0 ? n3.x : n3.y);
+        const uint32_t qhx = __float_as_uint(half == 0 ? n3.z : n3.w);
+        const uint32_t qhy = __float_as_uint(half == 0 ? n4.x : n4.y);
+        const uint32_t qhz = __float_as_uint(half == 0 ? n4.z : n4.w);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
+            const float x0 = fmaf(byte_to_float(qlx, j), sx, ax), x1 = fmaf(byte_to_float(qhx, j), sx, ax);
+            const float y0 = fmaf(byte_to_float(qly, j), sy, ay), y1 = fmaf(byte_to_float(qhy, j), sy, ay);
+            const float z0 = fmaf(byte_to_float(qlz, j), sz, az), z1 = fmaf(byte_to_float(qhz, j), sz, az);
+            const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+            const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
+            if (m != 0u && tn * kBoxLo <= tf * kBoxHi) {
+                const uint32_t child_bits = m >> 5;
+                const bool inner = (m & 0x18u) == 0x18u;
+                const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ octinv) : (m & 0x1Fu);
+                hitmask |= child_bits << bit_index;
+            }
+        }
+    }
+    return hitmask;
+}
+
+// Walks the compressed BVH8. Returns the BVH-order triangle index of the nearest hit in
+// [tmin, tmax) (ANY_HIT: of any hit) or -1. On a hit tmax is lowered to the hit distance.
+// stack_overflow is set (and the walk abandoned) if the tree is deeper than the stack.
+template <bool ANY_HIT, bool STATS>
+NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__ tris, int num_nodes,
+                    float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float& tmax,
+                    float& hu, float& hv, bool& stack_overflow, TraceStats* stats) {
+    if (num_nodes == 0) return -1;
+    const RayPre rp = ray_precompute(ox, oy, oz, dx, dy, dz);
+    // Clamp tiny direction components so the slab distances stay finite (no 0 * inf).
+    const float kTiny = 1e-20f;
+    const float idx_ = __frcp_rn(fabsf(dx) > kTiny ? dx : copysignf(kTiny, dx));
+    const float idy = __frcp_rn(fabsf(dy) > kTiny ? dy : copysignf(kTiny, dy));
+    const float idz = __frcp_rn(fabsf(dz) > kTiny ? dz : copysignf(kTiny, dz));
+    const uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    const uint32_t octinv = 7u - oct;
+
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    uint2 ngroup = make_uint2(0u, 0x80000000u);  // the root as the only internal hit, imask 0
+    int hit = -1;
+    while (true) {
+        // Visit the highest-priority internal child of the current group.
+        const uint32_t hits = ngroup.y;
+        const int bit = 31 - __clz(hits);
+        ngroup.y &= ~(1u << bit);
+        if (ngroup.y > 0x00FFFFFFu) {
+            if (sp == kTraversalStack) { stack_overflow = true; break; }
+            stack[sp++] = ngroup;
+        }
+        const uint32_t slot = (uint32_t)(bit - 24) ^ octinv;
+        const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+        const uint32_t node = ngroup.x + rel;
+        uint32_t child_base, tri_base, imask;
+        const uint32_t hm = intersect_children(nodes, node, ox, oy, oz, idx_, idy, idz, octinv, tmin, tmax,
+                                               child_base, tri_base, imask);
+        if (STATS) stats->nodes++;
+        ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
+        uint32_t tmask = hm & 0x00FFFFFFu;
+        while (tmask != 0u) {
+            const int tb = 31 - __clz(tmask);
+            tmask &= ~(1u << tb);
+            const uint32_t ti = tri_base + (uint32_t)tb;
+            const float4* tp = tris + 3 * (size_t)ti;
+            const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            if (STATS) stats->tris++;
+            float t, u, v;
+            if (tri_intersect(rp, p0, p1, p2, tmin, tmax, t, u, v)) {
+                tmax = t; hu = u; hv = v; hit = (int)ti;
+                if (ANY_HIT) return hit;
+            }
+        }
+        if (ngroup.y <= 0x00FFFFFFu) {
+            if (sp == 0) break;
+            ngroup = stack[--sp];
+        }
+    }
+    return hit;
+}
+
+}  // namespace ngi

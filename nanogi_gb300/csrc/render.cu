@@ -1,0 +1,954 @@
+// Wavefront path tracing on GB300: the `pt` and `ptdirect` estimators of
+// src/nanogi.cpp:446-607 and :609-802 reorganised as a persistent wave of path slots.
+//
+// One wave iteration = three kernels over HBM-resident SoA state:
+//   k_logic  : per slot, consume the previous extension hit (emission for pt, Russian
+//              roulette, vertex update), do next-event estimation (ptdirect) and sample the
+//              next direction; a finished slot immediately claims the next sample index
+//              (path regeneration) and starts a camera path. Extension and shadow rays are
+//              appended to compacted queues with one atomic per warp.
+//   k_extend : closest-hit traversal of the extension queue (compressed BVH8)
+//   k_shadow : any-hit traversal of the shadow queue; unoccluded contributions are added
+//              to the FP64 film with atomics.
+// Iterations are captured in a CUDA graph and replayed until every slot has drained.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device_scene.hpp"
+#include "ngi_shade.cuh"
+#include "ngi_trace.cuh"
+#include "scene.hpp"
+
+namespace ngi {
+
+#define CUDA_CHECK(x)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess)                                                                     \
+            throw DeviceError(std::string(cudaGetErrorString(e_)) + " (" #x ")",                   \
+                              e_ == cudaErrorMemoryAllocation ? NGI_ERR_OUT_OF_MEMORY : NGI_ERR_CUDA); \
+    } while (0)
+
+template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
+
+enum : uint8_t { SLOT_EMPTY = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
+
+struct WaveCounters {
+    unsigned long long next_sample;   // samples claimed so far (local index)
+    int ext_count;
+    int sh_count;
+    int active;
+    int error_flags;                  // bit 0: traversal stack overflow
+    unsigned long long stat_camera;
+    unsigned long long stat_ext;
+    unsigned long long stat_shadow;
+    unsigned long long stat_contrib;
+    unsigned long long stat_nonfinite;
+};
+
+struct RenderConsts {
+    int renderer;
+    int max_vertices;
+    long long num_samples;
+    long long sample_offset;
+    unsigned long long seed;
+    int width, height;
+    int stratified;
+    long long strat_end;    // global sample indices below this are pixel-stratified
+};
+
+template <typename R>
+struct WaveView {
+    int Q;
+    float4* ray_o;           // extension ray origin (xyz), tmin (w)
+    float4* ray_d;           // direction (xyz), tmax (w)
+    float4* hit;             // t, u, v, leaf-order triangle index (-1 = miss)
+    Vec4T<R>* thr;           // throughput
+    Vec4T<double>* od_o;     // FP64 path: exact origin
+    Vec4T<double>* od_d;     // FP64 path: exact direction
+    uint32_t* pixel;
+    unsigned long long* sample;
+    int* nverts;
+    uint8_t* state;
+    int* ext_queue;
+    float4* sh_o;
+    float4* sh_d;
+    Vec4T<R>* sh_c;
+    uint32_t* sh_pix;
+    WaveCounters* ctr;
+    double* film;
+};
+
+struct RenderWave {
+    int Q = 0;
+    int precision = -1;
+    std::vector<void*> bufs;
+    WaveCounters* ctr = nullptr;
+    WaveCounters* h_ctr = nullptr;   // pinned
+    WaveView<float> vf{};
+    WaveView<double> vd{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+// ---- warp helpers ----------------------------------------------------------------------
+NGI_D unsigned lane_id() { return threadIdx.x & 31u; }
+NGI_D unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// Warp-aggregated append: every lane of the warp calls this; returns the slot index for
+// lanes with want == true.
+NGI_D int warp_append(int* counter, bool want) {
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (mask == 0u) return -1;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return want ? base + __popc(mask & lanemask_lt()) : -1;
+}
+NGI_D void warp_add_u64(unsigned long long* counter, bool flag) {
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, flag);
+    if (mask != 0u && lane_id() == (unsigned)(__ffs(mask) - 1)) atomicAdd(counter, (unsigned long long)__popc(mask));
+}
+
+template <typename R>
+NGI_D bool finite3(V3<R> c) { return isfinite(c.x) && isfinite(c.y) && isfinite(c.z); }
+
+template <typename R>
+NGI_D void film_add(double* film, uint32_t pixel, V3<R> c) {
+    double* f = film + 3 * (size_t)pixel;
+    atomicAdd(f + 0, (double)c.x);
+    atomicAdd(f + 1, (double)c.y);
+    atomicAdd(f + 2, (double)c.z);
+}
+
+// A pending shadow ray held in registers until the warp appends it.
+template <typename R>
+struct ShadowRay {
+    bool valid;
+    float ox, oy, oz, dx, dy, dz, tmax;
+    V3<R> c;
+    uint32_t pixel;
+};
+
+// Next-event estimation at a vertex (src/nanogi.cpp:654-707).
+template <typename R>
+NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom<R>& g, bool at_sensor,
+                      const DevMaterial<R>* mat, V3<R> wi, V3<R> thr, uint32_t pixel, float4 u, ShadowRay<R>& out) {
+    out.valid = false;
+    const int nl = sv.num_lights;
+    int li = (int)((R)u.x * (R)nl);
+    li = li < 0 ? 0 : (li > nl - 1 ? nl - 1 : li);
+    const DevLight<R>& L = sv.lights[li];
+    if (L.type == LT_DIRECTIONAL) return;  // Le is 0 without forceDegenerated (rt.hpp:934-937)
+    Geom<R> gl;
+    R pdf_pos;
+    if (L.type == LT_AREA) {
+        sample_mesh_position(sv, L.tri_base, L.tri_count, L.cdf_offset, (R)u.y, (R)u.z, gl);
+        pdf_pos = L.inv_area;
+    } else {
+        gl.p = L.position;
+        gl.degenerated = true;
+        pdf_pos = R(1);
+    }
+    const V3<R> ppl = normalize(gl.p - g.p);
+    V3<R> fs_e;
+    if (at_sensor) {
+        if (sv.sensor.type == ET_PINHOLE) {
+            const R w = pinhole_importance(sv.sensor, ppl);
+            fs_e = v3<R>(w, w, w);
+        } else {
+            fs_e = dot(g.sn, ppl) > R(0) ? sv.sensor.We : v3<R>(0, 0, 0);
+        }
+    } else {
+        fs_e = bsdf_eval(*mat, g, wi, ppl, false);
+    }
+    if (is_zero(fs_e)) return;
+    V3<R> fs_l = L.Le;
+    if (L.type == LT_AREA && !(dot(gl.sn, -ppl) > R(0))) return;
+    const R G = geometry_term(g, gl);
+    const R pdf_l = R(1) / (R)nl;
+    const V3<R> C = thr * fs_e * G * fs_l / pdf_l / pdf_pos;
+    if (is_zero(C)) return;
+    uint32_t pix = pixel;
+    if (at_sensor) {
+        R rx, ry;
+        if (sv.sensor.type == ET_PINHOLE) {
+            pinhole_raster(sv.sensor, ppl, rx, ry);
+        } else {
+            rx = g.uvx; ry = g.uvy;
+        }
+        pix = (uint32_t)pixel_index(rx, ry, rc.width, rc.height);
+    }
+    // Scene::Visible (rt.hpp:2251-2261)
+    const V3<R> d = gl.p - g.p;
+    const R len = sqrt_(dot(d, d));
+    const V3<R> dn = d / len;
+    out.valid = true;
+    out.ox = (float)g.p.x; out.oy = (float)g.p.y; out.oz = (float)g.p.z;
+    out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
+    out.tmax = (float)len * (1.0f - kEpsF);
+    out.c = C;
+    out.pixel = pix;
+}
+
+template <typename R>
+NGI_D void store_ray(const WaveView<R>& w, int s, V3<R> o, V3<R> d) {
+    w.ray_o[s] = make_float4((float)o.x, (float)o.y, (float)o.z, kEpsF);
+    w.ray_d[s] = make_float4((float)d.x, (float)d.y, (float)d.z, kInfF);
+    if (sizeof(R) == 8) {
+        w.od_o[s] = Vec4T<double>{(double)o.x, (double)o.y, (double)o.z, 0.0};
+        w.od_d[s] = Vec4T<double>{(double)d.x, (double)d.y, (double)d.z, 0.0};
+    }
+}
+
+template <typename R, bool DIRECT>
+__global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
+        const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
+        uint8_t st = w.state[s];
+        bool need_new = st == SLOT_EMPTY;
+        bool want_ext = false;
+        ShadowRay<R> sa;
+        sa.valid = false;
+
+        if (st == SLOT_ACTIVE) {
+            // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
+            bool alive = false;
+            const float4 h = w.hit[s];
+            const int ti = __float_as_int(h.w);
+            if (ti >= 0) {
+                V3<R> o, d;
+                if (sizeof(R) == 8) {
+                    const Vec4T<double> a = w.od_o[s], b = w.od_d[s];
+                    o = v3<R>((R)a.x, (R)a.y, (R)a.z);
+                    d = v3<R>((R)b.x, (R)b.y, (R)b.z);
+                } else {
+                    const float4 a = w.ray_o[s], b = w.ray_d[s];
+                    o = v3<R>((R)a.x, (R)a.y, (R)a.z);
+                    d = v3<R>((R)b.x, (R)b.y, (R)b.z);
+                }
+                const Vec4T<R> t4 = w.thr[s];
+                V3<R> thr = v3<R>(t4.x, t4.y, t4.z);
+                const uint32_t pixel = w.pixel[s];
+                const unsigned long long sample = w.sample[s];
+                int nv = w.nverts[s];
+                const RngKey rk = make_rng(rc.seed, sample);
+
+                // Hit reconstruction (Scene::Intersect rt.hpp:2196-2233)
+                Geom<R> g;
+                g.p = o + d * (R)h.x;
+                const float4* tp = sv.tris + 3 * (size_t)ti;
+                const float4 q1 = tp[0], q2 = tp[1], q3 = tp[2];
+                const V3<R> p1 = v3<R>(q1.x, q1.y, q1.z), p2 = v3<R>(q2.x, q2.y, q2.z), p3 = v3<R>(q3.x, q3.y, q3.z);
+                g.gn = normalize(cross(p2 - p1, p3 - p1));
+                const float4* np = sv.nrm + 3 * (size_t)ti;
+                const float4 m1 = np[0], m2 = np[1], m3 = np[2];
+                const float bw = 1.0f - h.y - h.z;
+                g.sn = normalize(v3<R>(m1.x, m1.y, m1.z) * (R)bw + v3<R>(m2.x, m2.y, m2.z) * (R)h.y +
+                                 v3<R>(m3.x, m3.y, m3.z) * (R)h.z);
+                if (isnan_(g.sn.x) || isnan_(g.sn.y) || isnan_(g.sn.z)) g.sn = g.gn;
+                g.degenerated = false;
+                g.uvx = R(0); g.uvy = R(0);
+                const int prim = __float_as_int(m1.w);
+                const DevMaterial<R>& mat = sv.mats[prim];
+
+                if (!DIRECT && (mat.type & DT_L) && mat.l_type == LT_AREA) {
+                    // Emission on a light hit (src/nanogi.cpp:568-575)
+                    if (dot(g.sn, -d) > R(0)) {
+                        const V3<R> c = thr * mat.Le;
+                        if (!is_zero(c)) {
+                            if (finite3(c)) { film_add(w.film, pixel, c); atomicAdd(&w.ctr->stat_contrib, 1ull); }
+                            else atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                        }
+                    }
+                }
+                // Russian roulette after every hit (src/nanogi.cpp:583-591)
+                const float rr = rng4(rk, (uint32_t)nv, RNG_NEE_RR).w;
+                if (!(rr > 0.5f)) {
+                    thr = thr / R(0.5);
+                    nv++;
+                    if (!(rc.max_vertices != -1 && nv >= rc.max_vertices) && mat.bsdf != BSDF_NONE) {
+                        tangent_space(g);
+                        const V3<R> wi = -d;
+                        if (DIRECT) {
+                            const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
+                            next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
+                        }
+                        const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
+                        V3<R> wo;
+                        if (bsdf_sample(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo)) {
+                            const R pdf = bsdf_pdf(mat, g, wi, wo);
+                            const V3<R> fs = bsdf_eval(mat, g, wi, wo, true);
+                            if (!is_zero(fs)) {
+                                thr = thr * fs / pdf;
+                                store_ray(w, s, g.p, wo);
+                                w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+                                w.nverts[s] = nv;
+                                alive = true;
+                                want_ext = true;
+                            }
+                        }
+                    }
+                }
+            }
+            if (!alive) need_new = true;
+        }
+
+        // First shadow append (NEE of the vertex just processed)
+        {
+            const int q = warp_append(&w.ctr->sh_count, sa.valid);
+            if (sa.valid) {
+                w.sh_o[q] = make_float4(sa.ox, sa.oy, sa.oz, kEpsF);
+                w.sh_d[q] = make_float4(sa.dx, sa.dy, sa.dz, sa.tmax);
+                w.sh_c[q] = Vec4T<R>{sa.c.x, sa.c.y, sa.c.z, R(0)};
+                w.sh_pix[q] = sa.pixel;
+            }
+        }
+
+        // ---- claim a new sample for finished slots (path regeneration) ----
+        ShadowRay<R> sb;
+        sb.valid = false;
+        {
+            const unsigned mask = __ballot_sync(0xFFFFFFFFu, need_new);
+            unsigned long long k = 0;
+            if (mask != 0u) {
+                const int leader = __ffs(mask) - 1;
+                unsigned long long b = 0;
+                if ((int)lane_id() == leader) b = atomicAdd(&w.ctr->next_sample, (unsigned long long)__popc(mask));
+                b = __shfl_sync(0xFFFFFFFFu, b, leader);
+                k = b + (unsigned long long)__popc(mask & lanemask_lt());
+            }
+            if (need_new) {
+                if (k >= (unsigned long long)rc.num_samples) {
+                    st = SLOT_DONE;
+                } else {
+                    // ---- sensor vertex (src/nanogi.cpp:450-479, 609-641) ----
+                    const unsigned long long gsample = (unsigned long long)rc.sample_offset + k;
+                    const RngKey rk = make_rng(rc.seed, gsample);
+                    Geom<R> ge;
+                    V3<R> thr;
+                    const DevSensor<R>& cam = sv.sensor;
+                    bool ok = true;
+                    if (cam.type == ET_PINHOLE) {
+                        ge.p = cam.eye;
+                        ge.degenerated = true;
+                        ge.sn = ge.gn = ge.du = ge.dv = v3<R>(0, 0, 0);
+                        ge.uvx = ge.uvy = R(0);
+                        thr = v3<R>(1, 1, 1);
+                    } else {
+                        const float4 us = rng4(rk, 1u, RNG_SENSOR);
+                        sample_mesh_position(sv, cam.tri_base, cam.tri_count, cam.cdf_offset, (R)us.x, (R)us.y, ge);
+                        const R a = R(1) / cam.inv_area;
+                        thr = v3<R>(a, a, a);
+                    }
+                    if (DIRECT) {
+                        const float4 un = rng4(rk, 1u, RNG_NEE_RR);
+                        next_event(sv, rc, ge, true, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, 0u, un, sb);
+                    }
+                    const float4 ud = rng4(rk, 1u, RNG_DIR);
+                    V3<R> wo;
+                    uint32_t pix = 0;
+                    if (cam.type == ET_PINHOLE) {
+                        R rx, ry;
+                        if (rc.stratified && (long long)gsample < rc.strat_end) {
+                            const long long wh = (long long)rc.width * rc.height;
+                            const long long pidx = (long long)(gsample % (unsigned long long)wh);
+                            const int px = (int)(pidx % rc.width), py = (int)(pidx / rc.width);
+                            rx = ((R)px + (R)ud.x) / (R)rc.width;
+                            ry = ((R)py + (R)ud.y) / (R)rc.height;
+                        } else {
+                            rx = (R)ud.x;
+                            ry = (R)ud.y;
+                        }
+                        wo = pinhole_direction(cam, rx, ry);
+                        R qx, qy;
+                        if (!pinhole_raster(cam, wo, qx, qy)) ok = false;
+                        else {
+                            pix = (uint32_t)pixel_index(qx, qy, rc.width, rc.height);
+                            const R W = pinhole_importance(cam, wo);
+                            if (W == R(0)) ok = false;
+                            else thr = thr * (W / W);
+                        }
+                    } else {
+                        const V3<R> l = cosine_hemisphere((R)ud.x, (R)ud.y);
+                        wo = to_world(ge, l);
+                        pix = (uint32_t)pixel_index(ge.uvx, ge.uvy, rc.width, rc.height);
+                        const V3<R> lw = to_local(ge, wo);
+                        if (!(lw.z > R(0)) || is_zero(cam.We)) ok = false;
+                        else thr = thr * cam.We / kInvPi_<R>();
+                    }
+                    if (ok) {
+                        store_ray(w, s, ge.p, wo);
+                        w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+                        w.pixel[s] = pix;
+                        w.sample[s] = gsample;
+                        w.nverts[s] = 1;
+                        want_ext = true;
+                        st = SLOT_ACTIVE;
+                    } else {
+                        st = SLOT_EMPTY;
+                    }
+                }
+            }
+            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+        }
+        if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
+        if (want_ext) st = SLOT_ACTIVE;
+        w.state[s] = st;
+        {
+            const int q = warp_append(&w.ctr->sh_count, sb.valid);
+            if (sb.valid) {
+                w.sh_o[q] = make_float4(sb.ox, sb.oy, sb.oz, kEpsF);
+                w.sh_d[q] = make_float4(sb.dx, sb.dy, sb.dz, sb.tmax);
+                w.sh_c[q] = Vec4T<R>{sb.c.x, sb.c.y, sb.c.z, R(0)};
+                w.sh_pix[q] = sb.pixel;
+            }
+        }
+        {
+            const int q = warp_append(&w.ctr->ext_count, want_ext);
+            if (want_ext) w.ext_queue[q] = s;
+        }
+        {
+            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
+            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
+        }
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_extend(SceneView<R> sv, WaveView<R> w) {
+    const int n = w.ctr->ext_count;
+    bool overflow = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int s = w.ext_queue[i];
+        const float4 o = w.ray_o[s], d = w.ray_d[s];
+        float tmax = d.w, u = 0.0f, v = 0.0f;
+        const int ti = trace_ray<false, false>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
+                                               tmax, u, v, overflow, nullptr);
+        w.hit[s] = make_float4(tmax, u, v, __int_as_float(ti));
+    }
+    if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_ext, (unsigned long long)n);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_shadow(SceneView<R> sv, WaveView<R> w) {
+    const int n = w.ctr->sh_count;
+    bool overflow = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = w.sh_o[i], d = w.sh_d[i];
+        float tmax = d.w, u, v;
+        const int ti = trace_ray<true, false>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
+                                              tmax, u, v, overflow, nullptr);
+        if (ti < 0) {
+            const Vec4T<R> c = w.sh_c[i];
+            const V3<R> cc = v3<R>(c.x, c.y, c.z);
+            if (finite3(cc)) {
+                film_add(w.film, w.sh_pix[i], cc);
+                atomicAdd(&w.ctr->stat_contrib, 1ull);
+            } else {
+                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+            }
+        }
+    }
+    if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_shadow, (unsigned long long)n);
+}
+
+// ---- parity hooks --------------------------------------------------------------------------
+__global__ void k_intersect(const CwNode* nodes, const float4* tris, int num_nodes, const float4* rays, int64_t n,
+                            int32_t* prim, float* t_out, float* uv_out, int* err) {
+    bool overflow = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = rays[2 * i], b = rays[2 * i + 1];
+        float tmax = b.w, u = 0.0f, v = 0.0f;
+        const int ti = trace_ray<false, false>(nodes, tris, num_nodes, a.x, a.y, a.z, b.x, b.y, b.z, a.w, tmax, u, v,
+                                               overflow, nullptr);
+        prim[i] = ti >= 0 ? (int32_t)__float_as_uint(tris[3 * (size_t)ti].w) : -1;
+        t_out[i] = ti >= 0 ? tmax : INFINITY;
+        uv_out[2 * i] = ti >= 0 ? u : 0.0f;
+        uv_out[2 * i + 1] = ti >= 0 ? v : 0.0f;
+    }
+    if (overflow) atomicOr(err, 1);
+}
+
+__global__ void k_visible(const CwNode* nodes, const float4* tris, int num_nodes, const double* pts, int64_t n,
+                          uint8_t* vis, int* err) {
+    bool overflow = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double* p = pts + 6 * i;
+        const V3<double> a = v3<double>(p[0], p[1], p[2]), b = v3<double>(p[3], p[4], p[5]);
+        const V3<double> d = b - a;
+        const double len = sqrt(dot(d, d));
+        const V3<double> dn = d / len;
+        float tmax = (float)len * (1.0f - kEpsF), u, v;
+        const int ti = trace_ray<true, false>(nodes, tris, num_nodes, (float)a.x, (float)a.y, (float)a.z, (float)dn.x,
+                                              (float)dn.y, (float)dn.z, kEpsF, tmax, u, v, overflow, nullptr);
+        vis[i] = ti < 0 ? 1 : 0;
+    }
+    if (overflow) atomicOr(err, 1);
+}
+
+// ---- upload -----------------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+T* upload(const void* src, size_t count) {
+    T* p = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    CUDA_CHECK(cudaMalloc(&p, bytes));
+    if (count) CUDA_CHECK(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+}
+
+template <typename R> V3<R> hv3(const double a[3]) { return V3<R>{(R)a[0], (R)a[1], (R)a[2]}; }
+
+template <typename R>
+void build_tables(const HostScene& hs, std::vector<DevMaterial<R>>& mats, std::vector<DevLight<R>>& lights,
+                  DevSensor<R>& sensor, std::vector<double>& cdf, std::vector<float>& epos, std::vector<float>& euv) {
+    mats.clear();
+    lights.clear();
+    cdf.clear();
+    epos.clear();
+    euv.clear();
+    auto add_emitter_mesh = [&](const HostPrimitive& p, int& tri_base, int& cdf_off) {
+        tri_base = (int)(epos.size() / 9);
+        cdf_off = (int)cdf.size();
+        for (double v : p.area_cdf) cdf.push_back(v);
+        for (int64_t t = 0; t < p.tri_count; t++) {
+            for (int k = 0; k < 9; k++) epos.push_back(hs.tri_pos[9 * (p.tri_first + t) + k]);
+            for (int k = 0; k < 6; k++) euv.push_back(hs.tri_uv[6 * (p.tri_first + t) + k]);
+        }
+    };
+    for (size_t i = 0; i < hs.prims.size(); i++) {
+        const HostPrimitive& p = hs.prims[i];
+        DevMaterial<R> m{};
+        m.type = p.type;
+        m.bsdf = (p.type & PT_D) ? BSDF_D : (p.type & PT_G) ? BSDF_G : (p.type & PT_S) ? BSDF_S : BSDF_NONE;
+        m.s_type = p.s_type;
+        m.l_type = p.l_type;
+        m.R_ = m.bsdf == BSDF_D ? hv3<R>(p.D_R) : m.bsdf == BSDF_G ? hv3<R>(p.G_R) : hv3<R>(p.S_R);
+        m.eta = hv3<R>(p.G_eta);
+        m.k = hv3<R>(p.G_k);
+        m.roughness = (R)p.G_roughness;
+        m.eta1 = (R)p.S_eta1;
+        m.eta2 = (R)p.S_eta2;
+        m.Le = hv3<R>(p.Le);
+        m.light_index = -1;
+        mats.push_back(m);
+    }
+    for (size_t li = 0; li < hs.light_prims.size(); li++) {
+        const HostPrimitive& p = hs.prims[hs.light_prims[li]];
+        mats[hs.light_prims[li]].light_index = (int)li;
+        DevLight<R> L{};
+        L.type = p.l_type;
+        L.prim = hs.light_prims[li];
+        L.Le = hv3<R>(p.Le);
+        L.inv_area = (R)p.inv_area;
+        L.position = hv3<R>(p.l_position);
+        L.direction = hv3<R>(p.l_direction);
+        L.center = hv3<R>(p.l_center);
+        L.radius = (R)p.l_radius;
+        if (p.l_type == L_AREA) {
+            L.tri_count = (int)p.tri_count;
+            add_emitter_mesh(p, L.tri_base, L.cdf_offset);
+        }
+        lights.push_back(L);
+    }
+    sensor = DevSensor<R>{};
+    sensor.type = -1;
+    if (hs.sensor_prim >= 0) {
+        const HostPrimitive& p = hs.prims[hs.sensor_prim];
+        sensor.type = p.e_type;
+        sensor.prim = hs.sensor_prim;
+        sensor.eye = hv3<R>(p.eye);
+        sensor.Vx = hv3<R>(p.Vx);
+        sensor.Vy = hv3<R>(p.Vy);
+        sensor.Vz = hv3<R>(p.Vz);
+        sensor.tan_fov = (R)std::tan(p.fov * 0.5);
+        sensor.aspect = (R)p.aspect;
+        sensor.We = hv3<R>(p.We);
+        sensor.inv_area = (R)p.inv_area;
+        if (p.e_type == E_AREA) {
+            sensor.tri_count = (int)p.tri_count;
+            add_emitter_mesh(p, sensor.tri_base, sensor.cdf_offset);
+        }
+    }
+}
+
+template <typename R>
+SceneView<R> make_view(const DeviceScene& ds) {
+    SceneView<R> v{};
+    v.nodes = ds.nodes;
+    v.tris = ds.tris;
+    v.nrm = ds.nrm;
+    v.uv = ds.uv;
+    v.mats = (const DevMaterial<R>*)(sizeof(R) == 8 ? ds.mats_d : ds.mats_f);
+    v.lights = (const DevLight<R>*)(sizeof(R) == 8 ? ds.lights_d : ds.lights_f);
+    v.num_lights = ds.num_lights;
+    v.num_nodes = ds.num_nodes;
+    v.cdf = ds.cdf;
+    v.emit_tri_pos = ds.emit_pos;
+    v.emit_tri_uv = ds.emit_uv;
+    std::memcpy(&v.sensor, sizeof(R) == 8 ? ds.sensor_d : ds.sensor_f, sizeof(DevSensor<R>));
+    return v;
+}
+
+void free_wave(RenderWave* wv) {
+    if (!wv) return;
+    for (void* p : wv->bufs) cudaFree(p);
+    if (wv->h_ctr) cudaFreeHost(wv->h_ctr);
+    if (wv->ev0) cudaEventDestroy(wv->ev0);
+    if (wv->ev1) cudaEventDestroy(wv->ev1);
+    delete wv;
+}
+
+}  // namespace
+
+void DeviceUpload(HostScene& hs) {
+    if (hs.dev) return;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw DeviceError("no CUDA device is visible", NGI_ERR_NO_DEVICE);
+    }
+    static_assert(sizeof(DevSensor<double>) <= 256, "sensor record too large");
+    auto* ds = new DeviceScene();
+    hs.dev = ds;
+    try {
+        CUDA_CHECK(cudaGetDevice(&ds->device));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&ds->stream, cudaStreamNonBlocking));
+        const int n = (int)hs.NumTriangles();
+        ds->num_tris = n;
+        float* d_pos = upload<float>(hs.tri_pos.data(), hs.tri_pos.size());
+        float* d_nrm = upload<float>(hs.tri_nrm.data(), hs.tri_nrm.size());
+        float* d_uv = upload<float>(hs.tri_uv.data(), hs.tri_uv.size());
+        int* d_prim = upload<int>(hs.tri_prim.data(), hs.tri_prim.size());
+        try {
+            BuildBvh(*ds, d_pos, d_nrm, d_uv, d_prim, n, ds->stream);
+        } catch (...) {
+            cudaFree(d_pos); cudaFree(d_nrm); cudaFree(d_uv); cudaFree(d_prim);
+            throw;
+        }
+        cudaFree(d_pos); cudaFree(d_nrm); cudaFree(d_uv); cudaFree(d_prim);
+        if (ds->bvh_depth > kTraversalStack)
+            throw DeviceError("BVH depth " + std::to_string(ds->bvh_depth) + " exceeds the traversal stack", NGI_ERR_UNSUPPORTED);
+
+        std::vector<DevMaterial<float>> mf; std::vector<DevLight<float>> lf; DevSensor<float> sf;
+        std::vector<DevMaterial<double>> md; std::vector<DevLight<double>> ld; DevSensor<double> sd;
+        std::vector<double> cdf; std::vector<float> epos, euv;
+        build_tables<float>(hs, mf, lf, sf, cdf, epos, euv);
+        build_tables<double>(hs, md, ld, sd, cdf, epos, euv);
+        ds->mats_f = upload<DevMaterial<float>>(mf.data(), mf.size());
+        ds->mats_d = upload<DevMaterial<double>>(md.data(), md.size());
+        ds->lights_f = upload<DevLight<float>>(lf.data(), lf.size());
+        ds->lights_d = upload<DevLight<double>>(ld.data(), ld.size());
+        ds->cdf = upload<double>(cdf.data(), cdf.size());
+        ds->emit_pos = upload<float>(epos.data(), epos.size());
+        ds->emit_uv = upload<float>(euv.data(), euv.size());
+        ds->num_lights = (int)lf.size();
+        std::memcpy(ds->sensor_f, &sf, sizeof(sf));
+        std::memcpy(ds->sensor_d, &sd, sizeof(sd));
+        CUDA_CHECK(cudaStreamSynchronize(ds->stream));
+    } catch (...) {
+        DeviceFree(hs);
+        throw;
+    }
+}
+
+void DeviceFree(HostScene& hs) {
+    DeviceScene* ds = hs.dev;
+    if (!ds) return;
+    if (ds->stream) cudaStreamSynchronize(ds->stream);
+    free_wave(ds->wave);
+    void* ptrs[] = {ds->nodes, ds->tris, ds->nrm, ds->uv, ds->mats_f, ds->mats_d, ds->lights_f,
+                    ds->lights_d, ds->cdf, ds->emit_pos, ds->emit_uv, ds->film};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (ds->stream) cudaStreamDestroy(ds->stream);
+    delete ds;
+    hs.dev = nullptr;
+}
+
+// ---- render driver ------------------------------------------------------------------------------
+namespace {
+
+template <typename R>
+void alloc_wave_view(RenderWave* wv, WaveView<R>& v, int Q) {
+    auto A = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+        wv->bufs.push_back(p);
+        return p;
+    };
+    v.Q = Q;
+    v.ray_o = (float4*)A(sizeof(float4) * Q);
+    v.ray_d = (float4*)A(sizeof(float4) * Q);
+    v.hit = (float4*)A(sizeof(float4) * Q);
+    v.thr = (Vec4T<R>*)A(sizeof(Vec4T<R>) * Q);
+    if (sizeof(R) == 8) {
+        v.od_o = (Vec4T<double>*)A(sizeof(Vec4T<double>) * Q);
+        v.od_d = (Vec4T<double>*)A(sizeof(Vec4T<double>) * Q);
+    } else {
+        v.od_o = v.od_d = nullptr;
+    }
+    v.pixel = (uint32_t*)A(sizeof(uint32_t) * Q);
+    v.sample = (unsigned long long*)A(sizeof(unsigned long long) * Q);
+    v.nverts = (int*)A(sizeof(int) * Q);
+    v.state = (uint8_t*)A(sizeof(uint8_t) * Q);
+    v.ext_queue = (int*)A(sizeof(int) * Q);
+    v.sh_o = (float4*)A(sizeof(float4) * 2 * (size_t)Q);
+    v.sh_d = (float4*)A(sizeof(float4) * 2 * (size_t)Q);
+    v.sh_c = (Vec4T<R>*)A(sizeof(Vec4T<R>) * 2 * (size_t)Q);
+    v.sh_pix = (uint32_t*)A(sizeof(uint32_t) * 2 * (size_t)Q);
+    v.ctr = wv->ctr;
+}
+
+RenderWave* ensure_wave(DeviceScene& ds, int Q, int precision) {
+    if (ds.wave && ds.wave->Q == Q && ds.wave->precision == precision) return ds.wave;
+    free_wave(ds.wave);
+    ds.wave = nullptr;
+    auto* wv = new RenderWave();
+    try {
+        wv->Q = Q;
+        wv->precision = precision;
+        void* c = nullptr;
+        CUDA_CHECK(cudaMalloc(&c, sizeof(WaveCounters)));
+        wv->bufs.push_back(c);
+        wv->ctr = (WaveCounters*)c;
+        CUDA_CHECK(cudaMallocHost(&wv->h_ctr, sizeof(WaveCounters)));
+        if (precision == NGI_PRECISION_FP64) alloc_wave_view<double>(wv, wv->vd, Q);
+        else alloc_wave_view<float>(wv, wv->vf, Q);
+        CUDA_CHECK(cudaEventCreate(&wv->ev0));
+        CUDA_CHECK(cudaEventCreate(&wv->ev1));
+    } catch (...) {
+        free_wave(wv);
+        throw;
+    }
+    ds.wave = wv;
+    return wv;
+}
+
+int grid_for(int items, int block) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int max_blocks = sms * 8;  // persistent-style: 8 x 256 threads resident per SM
+    return std::max(1, std::min(max_blocks, (items + block - 1) / block));
+}
+
+template <typename R, bool DIRECT>
+void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
+              cudaStream_t stream) {
+    DeviceScene& ds = *hs.dev;
+    const SceneView<R> sv = make_view<R>(ds);
+    const int block = 256;
+    const int g_logic = grid_for(v.Q, block);
+    const int g_trace = grid_for(2 * v.Q, block);
+    const size_t ctr_reset_off = offsetof(WaveCounters, ext_count);
+    const size_t ctr_reset_len = offsetof(WaveCounters, error_flags) - ctr_reset_off;
+
+    CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
+    CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < iters_per_graph; it++) {
+        cudaMemsetAsync((char*)wv->ctr + ctr_reset_off, 0, ctr_reset_len, stream);
+        k_logic<R, DIRECT><<<g_logic, block, 0, stream>>>(sv, v, rc);
+        k_extend<R><<<g_trace, block, 0, stream>>>(sv, v);
+        k_shadow<R><<<g_trace, block, 0, stream>>>(sv, v);
+    }
+    const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
+    if (cap != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        throw DeviceError(std::string("graph capture failed: ") + cudaGetErrorString(cap));
+    }
+    const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
+
+    long long iterations = 0;
+    // Each path ends within (max vertices) iterations after it starts; the bound below is
+    // generous and only guards against a logic error spinning forever.
+    const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
+    const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
+    try {
+        CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
+        while (true) {
+            CUDA_CHECK(cudaGraphLaunch(exec, stream));
+            iterations += iters_per_graph;
+            CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, stream));
+            CUDA_CHECK(cudaStreamSynchronize(stream));
+            if (wv->h_ctr->error_flags & 1)
+                throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+            if (wv->h_ctr->active == 0 && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples) break;
+            if (iterations > max_iters) throw DeviceError("wave did not drain", NGI_ERR_DEVICE_TIMEOUT);
+        }
+        CUDA_CHECK(cudaEventRecord(wv->ev1, stream));
+        CUDA_CHECK(cudaEventSynchronize(wv->ev1));
+    } catch (...) {
+        cudaStreamSynchronize(stream);
+        cudaGraphExecDestroy(exec);
+        throw;
+    }
+    cudaGraphExecDestroy(exec);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, wv->ev0, wv->ev1);
+    const WaveCounters& c = *wv->h_ctr;
+    ds.last_stats.camera_rays = (int64_t)c.stat_camera;
+    ds.last_stats.extension_rays = (int64_t)c.stat_ext;
+    ds.last_stats.shadow_rays = (int64_t)c.stat_shadow;
+    ds.last_stats.film_contributions = (int64_t)c.stat_contrib;
+    ds.last_stats.nonfinite = (int64_t)c.stat_nonfinite;
+    ds.last_stats.iterations = iterations;
+    ds.last_stats.render_ms = ms;
+}
+
+}  // namespace
+
+void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cudaStream_t user_stream) {
+    DeviceUpload(hs);
+    DeviceScene& ds = *hs.dev;
+    if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
+    if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
+        throw DeviceError("ptdirect needs at least one light (the reference indexes an empty light list)",
+                          NGI_ERR_UNSUPPORTED);
+    cudaStream_t stream = user_stream ? user_stream : ds.stream;
+    ds.last_stats = ngi_render_stats{};
+    if (p.num_samples == 0) return;
+    int Q = p.wave_size > 0 ? p.wave_size : (1 << 21);
+    const long long need = std::max<long long>(p.num_samples, 256);
+    if ((long long)Q > need) Q = (int)need;
+    Q = (Q + 255) / 256 * 256;
+    RenderWave* wv = ensure_wave(ds, Q, p.precision);
+    RenderConsts rc{};
+    rc.renderer = p.renderer;
+    rc.max_vertices = p.max_num_vertices;
+    rc.num_samples = p.num_samples;
+    rc.sample_offset = p.sample_offset;
+    rc.seed = p.seed;
+    rc.width = p.width;
+    rc.height = p.height;
+    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
+    const long long wh = (long long)p.width * p.height;
+    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
+    if (p.precision == NGI_PRECISION_FP64) {
+        WaveView<double> v = wv->vd;
+        v.film = d_film;
+        if (p.renderer == NGI_RENDERER_PTDIRECT) run_wave<double, true>(hs, wv, v, rc, ipg, stream);
+        else run_wave<double, false>(hs, wv, v, rc, ipg, stream);
+    } else {
+        WaveView<float> v = wv->vf;
+        v.film = d_film;
+        if (p.renderer == NGI_RENDERER_PTDIRECT) run_wave<float, true>(hs, wv, v, rc, ipg, stream);
+        else run_wave<float, false>(hs, wv, v, rc, ipg, stream);
+    }
+}
+
+__global__ void k_scale(double* film, size_t n, double s) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        film[i] *= s;
+}
+
+void DeviceRenderToHost(HostScene& hs, const ngi_render_params& p, double* h_film) {
+    DeviceUpload(hs);
+    DeviceScene& ds = *hs.dev;
+    const size_t elems = 3 * (size_t)p.width * (size_t)p.height;
+    if (ds.film_elems < elems) {
+        if (ds.film) cudaFree(ds.film);
+        ds.film = nullptr;
+        ds.film_elems = 0;
+        CUDA_CHECK(cudaMalloc(&ds.film, elems * sizeof(double)));
+        ds.film_elems = elems;
+    }
+    CUDA_CHECK(cudaMemsetAsync(ds.film, 0, elems * sizeof(double), ds.stream));
+    DeviceRender(hs, p, ds.film, ds.stream);
+    if (p.num_samples > 0) {
+        // RenderProcess gather: film *= W*H / processedSamples (src/nanogi.cpp:434-437)
+        const double scale = (double)p.width * (double)p.height / (double)p.num_samples;
+        k_scale<<<grid_for((int)std::min<size_t>(elems, 1u << 30), 256), 256, 0, ds.stream>>>(ds.film, elems, scale);
+        CUDA_CHECK(cudaGetLastError());
+    }
+    CUDA_CHECK(cudaMemcpyAsync(h_film, ds.film, elems * sizeof(double), cudaMemcpyDeviceToHost, ds.stream));
+    CUDA_CHECK(cudaStreamSynchronize(ds.stream));
+}
+
+void DeviceIntersect(HostScene& hs, const float* h_rays, int64_t n, int32_t* prim, float* t, float* uv) {
+    DeviceUpload(hs);
+    DeviceScene& ds = *hs.dev;
+    if (n == 0) return;
+    float4* d_rays = nullptr;
+    int32_t* d_prim = nullptr;
+    float *d_t = nullptr, *d_uv = nullptr;
+    int* d_err = nullptr;
+    auto cleanup = [&]() { cudaFree(d_rays); cudaFree(d_prim); cudaFree(d_t); cudaFree(d_uv); cudaFree(d_err); };
+    try {
+        CUDA_CHECK(cudaMalloc(&d_rays, sizeof(float4) * 2 * n));
+        CUDA_CHECK(cudaMalloc(&d_prim, sizeof(int32_t) * n));
+        CUDA_CHECK(cudaMalloc(&d_t, sizeof(float) * n));
+        CUDA_CHECK(cudaMalloc(&d_uv, sizeof(float) * 2 * n));
+        CUDA_CHECK(cudaMalloc(&d_err, sizeof(int)));
+        CUDA_CHECK(cudaMemsetAsync(d_err, 0, sizeof(int), ds.stream));
+        CUDA_CHECK(cudaMemcpyAsync(d_rays, h_rays, sizeof(float) * 8 * n, cudaMemcpyHostToDevice, ds.stream));
+        const int block = 256;
+        const int grid = (int)std::min<int64_t>((n + block - 1) / block, 152 * 16);
+        k_intersect<<<grid, block, 0, ds.stream>>>(ds.nodes, ds.tris, ds.num_nodes, d_rays, n, d_prim, d_t, d_uv, d_err);
+        CUDA_CHECK(cudaGetLastError());
+        int err = 0;
+        CUDA_CHECK(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ds.stream));
+        std::vector<int32_t> hp(prim ? 0 : n);
+        std::vector<float> ht(t ? 0 : n), huv(uv ? 0 : 2 * n);
+        CUDA_CHECK(cudaMemcpyAsync(prim ? prim : hp.data(), d_prim, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ds.stream));
+        CUDA_CHECK(cudaMemcpyAsync(t ? t : ht.data(), d_t, sizeof(float) * n, cudaMemcpyDeviceToHost, ds.stream));
+        CUDA_CHECK(cudaMemcpyAsync(uv ? uv : huv.data(), d_uv, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, ds.stream));
+        CUDA_CHECK(cudaStreamSynchronize(ds.stream));
+        if (err) throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+    } catch (...) {
+        cudaStreamSynchronize(ds.stream);
+        cleanup();
+        throw;
+    }
+    cleanup();
+}
+
+void DeviceVisible(HostScene& hs, const double* h_pts, int64_t n, uint8_t* vis) {
+    DeviceUpload(hs);
+    DeviceScene& ds = *hs.dev;
+    if (n == 0) return;
+    double* d_pts = nullptr;
+    uint8_t* d_vis = nullptr;
+    int* d_err = nullptr;
+    auto cleanup = [&]() { cudaFree(d_pts); cudaFree(d_vis); cudaFree(d_err); };
+    try {
+        CUDA_CHECK(cudaMalloc(&d_pts, sizeof(double) * 6 * n));
+        CUDA_CHECK(cudaMalloc(&d_vis, n));
+        CUDA_CHECK(cudaMalloc(&d_err, sizeof(int)));
+        CUDA_CHECK(cudaMemsetAsync(d_err, 0, sizeof(int), ds.stream));
+        CUDA_CHECK(cudaMemcpyAsync(d_pts, h_pts, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, ds.stream));
+        const int block = 256;
+        const int grid = (int)std::min<int64_t>((n + block - 1) / block, 152 * 16);
+        k_visible<<<grid, block, 0, ds.stream>>>(ds.nodes, ds.tris, ds.num_nodes, d_pts, n, d_vis, d_err);
+        CUDA_CHECK(cudaGetLastError());
+        int err = 0;
+        CUDA_CHECK(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ds.stream));
+        CUDA_CHECK(cudaMemcpyAsync(vis, d_vis, n, cudaMemcpyDeviceToHost, ds.stream));
+        CUDA_CHECK(cudaStreamSynchronize(ds.stream));
+        if (err) throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+    } catch (...) {
+        cudaStreamSynchronize(ds.stream);
+        cleanup();
+        throw;
+    }
+    cleanup();
+}
+
+}  // namespace ngi

@@ -1,0 +1,407 @@
+"""Seeded synthetic scenes in nanogi's scene format (YAML version 5 + one OBJ per primitive).
+
+Every scene is first built in memory as a ``SceneDesc`` (float32 vertex arrays exactly as
+they are written to the OBJ files, plus the per-primitive parameters of schema.yml), then
+written to disk. Tests hand the same in-memory description to the CPU oracle, so the
+product's YAML/OBJ loader is checked against data it never parsed.
+
+Workloads (sizes from the benchmark configurations):
+* ``cornell_box``   -- open unit box, 5 wall quads, two rotated boxes, 0.25 x 0.25 ceiling
+                       light of radiance (17, 12, 4): 36 triangles.
+* ``terrain_scene`` -- 512 x 512 fBm height field (seeded value noise, 6 octaves), 200
+                       level-4 icospheres (5120 triangles each) of log-uniform radius
+                       0.05-1 with diffuse / glossy / mirror / glass materials drawn
+                       uniformly, 4 quad lights of radiance U[5, 20]: ~1.55 M triangles.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+# Conductor constants used for every glossy (G) material: published optical constants of
+# gold at (650, 550, 450) nm.
+GOLD_ETA = (0.14, 0.129, 0.1585)
+GOLD_K = (4.58625, 3.348125, 2.329375)
+
+
+@dataclass
+class Mesh:
+    positions: np.ndarray          # (V, 3) float32
+    normals: np.ndarray            # (V, 3) float32
+    faces: np.ndarray              # (F, 3) int64, 0-based
+    uvs: np.ndarray | None = None  # (V, 2) float32
+
+
+@dataclass
+class Primitive:
+    type: list[str]
+    params: dict
+    mesh: Mesh | None = None
+    name: str = "prim"
+
+
+@dataclass
+class SceneDesc:
+    primitives: list[Primitive] = field(default_factory=list)
+
+    @property
+    def num_triangles(self) -> int:
+        return sum(len(p.mesh.faces) for p in self.primitives if p.mesh is not None)
+
+
+# ---- mesh helpers ------------------------------------------------------------------------------
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).astype(np.float32))
+
+
+def quad(p0, p1, p2, p3, normal) -> Mesh:
+    """Quad p0-p1-p2-p3 (counter-clockwise seen from `normal`) as two triangles."""
+    P = _f32([p0, p1, p2, p3])
+    N = _f32([normal] * 4)
+    F = np.array([[0, 1, 2], [0, 2, 3]], np.int64)
+    return Mesh(P, N, F, _f32([[0, 0], [1, 0], [1, 1], [0, 1]]))
+
+
+def box(center, size, angle_deg) -> Mesh:
+    """Axis-aligned box rotated about +y, 6 faces x 2 triangles, outward flat normals."""
+    cx, cy, cz = center
+    sx, sy, sz = size
+    a = math.radians(angle_deg)
+    ca, sa = math.cos(a), math.sin(a)
+
+    def tr(x, y, z):
+        return (cx + ca * x + sa * z, cy + y, cz - sa * x + ca * z)
+
+    def rn(nx, ny, nz):
+        return (ca * nx + sa * nz, ny, -sa * nx + ca * nz)
+
+    hx, hy, hz = sx / 2, sy / 2, sz / 2
+    faces = [
+        ((-hx, -hy, hz), (hx, -hy, hz), (hx, hy, hz), (-hx, hy, hz), (0, 0, 1)),
+        ((hx, -hy, -hz), (-hx, -hy, -hz), (-hx, hy, -hz), (hx, hy, -hz), (0, 0, -1)),
+        ((hx, -hy, hz), (hx, -hy, -hz), (hx, hy, -hz), (hx, hy, hz), (1, 0, 0)),
+        ((-hx, -hy, -hz), (-hx, -hy, hz), (-hx, hy, hz), (-hx, hy, -hz), (-1, 0, 0)),
+        ((-hx, hy, hz), (hx, hy, hz), (hx, hy, -hz), (-hx, hy, -hz), (0, 1, 0)),
+        ((-hx, -hy, -hz), (hx, -hy, -hz), (hx, -hy, hz), (-hx, -hy, hz), (0, -1, 0)),
+    ]
+    P, N, F = [], [], []
+    for q0, q1, q2, q3, n in faces:
+        b = len(P)
+        P += [tr(*q0), tr(*q1), tr(*q2), tr(*q3)]
+        N += [rn(*n)] * 4
+        F += [[b, b + 1, b + 2], [b, b + 2, b + 3]]
+    return Mesh(_f32(P), _f32(N), np.array(F, np.int64))
+
+
+def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere: (V, 3) float64 vertices, (F, 3) faces, outward winding."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(level):
+        cache: dict[tuple[int, int], int] = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts), np.array(faces, np.int64)
+
+
+_ICO_CACHE: dict[int, tuple[np.ndarray, np.ndarray]] = {}
+
+
+def sphere_mesh(center, radius, level=4) -> Mesh:
+    if level not in _ICO_CACHE:
+        _ICO_CACHE[level] = icosphere(level)
+    V, F = _ICO_CACHE[level]
+    P = _f32(V * radius + np.asarray(center, np.float64))
+    return Mesh(P, _f32(V), F.copy())
+
+
+# ---- materials -------------------------------------------------------------------------------------
+def diffuse(r) -> tuple[list[str], dict]:
+    return ["D"], {"D": {"R": [float(x) for x in r]}}
+
+
+def glossy(r, roughness) -> tuple[list[str], dict]:
+    return ["G"], {"G": {"R": [float(x) for x in r], "Eta": list(GOLD_ETA), "K": list(GOLD_K),
+                         "Roughness": float(roughness)}}
+
+
+def mirror(r=(1.0, 1.0, 1.0)) -> tuple[list[str], dict]:
+    return ["S"], {"S": {"type": "reflection", "reflection": {"R": [float(x) for x in r]}}}
+
+
+def glass(eta2=1.5, r=(1.0, 1.0, 1.0)) -> tuple[list[str], dict]:
+    return ["S"], {"S": {"type": "fresnel", "fresnel": {"R": [float(x) for x in r], "eta1": 1.0, "eta2": float(eta2)}}}
+
+
+def area_light(le) -> tuple[list[str], dict]:
+    # Light primitives carry a black diffuse BSDF, as the reference's own scenes do: a pure
+    # [L] primitive reaches assert(0) in SampleDirection after a hit (rt.hpp:909).
+    return ["L", "D"], {"L": {"type": "area", "area": {"Le": [float(x) for x in le]}}, "D": {"R": [0.0, 0.0, 0.0]}}
+
+
+def pinhole(eye, center, up, fov) -> Primitive:
+    return Primitive(["E"], {"E": {"type": "pinhole", "pinhole": {
+        "We": [1.0, 1.0, 1.0], "view": {"eye": [float(x) for x in eye], "center": [float(x) for x in center],
+                                         "up": [float(x) for x in up]},
+        "perspective": {"fov": float(fov)}}}}, None, "camera")
+
+
+def phong_to_beckmann(n: float) -> float:
+    """Beckmann roughness matching a Phong lobe exponent (Walter et al. 2007): sqrt(2/(n+2))."""
+    return math.sqrt(2.0 / (n + 2.0))
+
+
+# ---- workloads -------------------------------------------------------------------------------------
+def cornell_box(light_le=(17.0, 12.0, 4.0)) -> SceneDesc:
+    """Open unit box [0,1]^3 (front face z=1 open), camera outside looking in -z."""
+    s = SceneDesc()
+    grey, red, green = (0.73, 0.73, 0.73), (0.63, 0.065, 0.05), (0.14, 0.45, 0.09)
+    walls = [
+        ("floor", quad((0, 0, 1), (1, 0, 1), (1, 0, 0), (0, 0, 0), (0, 1, 0)), grey),
+        ("ceiling", quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1), (0, -1, 0)), grey),
+        ("back", quad((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1)), grey),
+        ("left", quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0)), red),
+        ("right", quad((1, 0, 1), (1, 1, 1), (1, 1, 0), (1, 0, 0), (-1, 0, 0)), green),
+    ]
+    lt, lp = area_light(light_le)
+    h = 1.0 - 1e-3
+    s.primitives.append(Primitive(lt, lp, quad((0.375, h, 0.375), (0.625, h, 0.375), (0.625, h, 0.625),
+                                                (0.375, h, 0.625), (0, -1, 0)), "light"))
+    for name, m, col in walls:
+        t, p = diffuse(col)
+        s.primitives.append(Primitive(t, p, m, name))
+    t, p = diffuse(grey)
+    s.primitives.append(Primitive(t, p, box((0.33, 0.3, 0.37), (0.3, 0.6, 0.3), 15.0), "tallbox"))
+    s.primitives.append(Primitive(list(t), dict(p), box((0.68, 0.15, 0.65), (0.3, 0.3, 0.3), -18.0), "shortbox"))
+    s.primitives.append(pinhole((0.5, 0.5, 2.4), (0.5, 0.5, 0.0), (0, 1, 0), 36.0))
+    return s
+
+
+def _value_noise_fbm(x: np.ndarray, z: np.ndarray, seed: int, octaves: int = 6) -> np.ndarray:
+    """Fractional Brownian motion of seeded value noise (smoothstep-interpolated lattice)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros_like(x)
+    amp, freq, norm = 1.0, 1.0, 0.0
+    for _ in range(octaves):
+        lat = rng.random((257, 257)) * 2.0 - 1.0
+        gx, gz = x * freq, z * freq
+        ix, iz = np.floor(gx).astype(np.int64), np.floor(gz).astype(np.int64)
+        fx, fz = gx - ix, gz - iz
+        sx, sz = fx * fx * (3 - 2 * fx), fz * fz * (3 - 2 * fz)
+        ix, iz = ix % 256, iz % 256
+        v00, v10 = lat[ix, iz], lat[ix + 1, iz]
+        v01, v11 = lat[ix, iz + 1], lat[ix + 1, iz + 1]
+        out += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sz) + (v01 * (1 - sx) + v11 * sx) * sz)
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return out / norm
+
+
+def terrain_mesh(grid: int = 512, extent: float = 16.0, height: float = 1.5, seed: int = 2) -> tuple[Mesh, callable]:
+    xs = np.linspace(-extent / 2, extent / 2, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    base = 0.35  # lattice frequency in cells per scene unit
+    H = height * _value_noise_fbm((X + extent) * base, (Z + extent) * base, seed)
+    P = np.stack([X, H, Z], -1).reshape(-1, 3)
+    # vertex normals from central differences of the height field
+    dx = xs[1] - xs[0]
+    gx = np.gradient(H, dx, axis=0)
+    gz = np.gradient(H, dx, axis=1)
+    Nn = np.stack([-gx, np.ones_like(H), -gz], -1)
+    Nn /= np.linalg.norm(Nn, axis=-1, keepdims=True)
+    idx = np.arange(grid * grid).reshape(grid, grid)
+    a, b = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel()
+    c, d = idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+    # winding so that cross(p2-p1, p3-p1) points up (+y)
+    F = np.concatenate([np.stack([a, d, c], -1), np.stack([a, c, b], -1)])
+
+    def height_at(x, z):
+        return float(height * _value_noise_fbm(np.array([(x + extent) * base]), np.array([(z + extent) * base]), seed)[0])
+
+    return Mesh(_f32(P), _f32(Nn.reshape(-1, 3)), F.astype(np.int64)), height_at
+
+
+def terrain_scene(num_spheres: int = 200, grid: int = 512, level: int = 4, seed_terrain: int = 2,
+                  seed_spheres: int = 3) -> SceneDesc:
+    """The ~1.55 M-triangle ptdirect workload."""
+    s = SceneDesc()
+    extent = 16.0
+    terrain, height_at = terrain_mesh(grid, extent, 1.5, seed_terrain)
+    rng = np.random.default_rng(seed_spheres)
+    lrng = np.random.default_rng(seed_spheres + 1000)
+    # 4 quad lights of radiance U[5, 20] above the terrain, facing down
+    for i, (lx, lz) in enumerate([(-4.0, -3.0), (4.0, -3.0), (-4.0, 4.0), (4.0, 4.0)]):
+        le = lrng.uniform(5.0, 20.0, 3)
+        hs, y = 0.9, 7.0
+        t, p = area_light(le)
+        s.primitives.append(Primitive(t, p, quad((lx - hs, y, lz - hs), (lx + hs, y, lz - hs), (lx + hs, y, lz + hs),
+                                                 (lx - hs, y, lz + hs), (0, -1, 0)), f"light{i}"))
+    t, p = diffuse((0.45, 0.5, 0.4))
+    s.primitives.append(Primitive(t, p, terrain, "terrain"))
+    for i in range(num_spheres):
+        r = float(math.exp(rng.uniform(math.log(0.05), math.log(1.0))))
+        x, z = rng.uniform(-extent / 2 + 1, extent / 2 - 1, 2)
+        y = height_at(x, z) + r
+        kind = int(rng.integers(0, 4))
+        if kind == 0:
+            t, p = diffuse(rng.uniform(0.1, 0.9, 3))
+        elif kind == 1:
+            n = float(math.exp(rng.uniform(math.log(10.0), math.log(1000.0))))
+            t, p = glossy(rng.uniform(0.5, 1.0, 3), phong_to_beckmann(n))
+        elif kind == 2:
+            t, p = mirror((0.95, 0.95, 0.95))
+        else:
+            t, p = glass(1.5)
+        s.primitives.append(Primitive(t, p, sphere_mesh((x, y, z), r, level), f"sphere{i}"))
+    s.primitives.append(pinhole((0.0, 7.5, 13.0), (0.0, 0.0, 0.0), (0, 1, 0), 45.0))
+    return s
+
+
+# ---- writers --------------------------------------------------------------------------------------------
+def _fmt_rows(prefix: str, a: np.ndarray) -> str:
+    # '%.9g' round-trips float32 exactly
+    a = np.asarray(a)
+    if a.dtype.kind == "f":
+        cols = [np.char.mod("%.9g", a[:, k].astype(np.float64)) for k in range(a.shape[1])]
+    else:
+        cols = [a[:, k].astype(str) for k in range(a.shape[1])]
+    out = np.char.add(prefix, cols[0])
+    for c in cols[1:]:
+        out = np.char.add(np.char.add(out, " "), c)
+    return "\n".join(out.tolist()) + "\n"
+
+
+def write_obj(path: Path, m: Mesh, name: str) -> None:
+    parts = [f"o {name}\n", _fmt_rows("v ", m.positions)]
+    if m.uvs is not None:
+        parts.append(_fmt_rows("vt ", m.uvs))
+    parts.append(_fmt_rows("vn ", m.normals))
+    f1 = (m.faces + 1).astype(np.int64)
+    if m.uvs is not None:
+        idx = [np.char.add(np.char.add(np.char.add(np.char.add(f1[:, k].astype(str), "/"), f1[:, k].astype(str)), "/"),
+                           f1[:, k].astype(str)) for k in range(3)]
+    else:
+        idx = [np.char.add(np.char.add(f1[:, k].astype(str), "//"), f1[:, k].astype(str)) for k in range(3)]
+    lines = np.char.add(np.char.add(np.char.add(np.char.add(np.char.add("f ", idx[0]), " "), idx[1]), " "), idx[2])
+    parts.append("\n".join(lines.tolist()) + "\n")
+    Path(path).write_text("".join(parts))
+
+
+def _yaml_value(v, indent: int) -> str:
+    pad = " " * indent
+    if isinstance(v, dict):
+        out = ""
+        for k, x in v.items():
+            if isinstance(x, dict):
+                out += f"{pad}{k}:\n" + _yaml_value(x, indent + 2)
+            else:
+                out += f"{pad}{k}: {_yaml_scalar(x)}\n"
+        return out
+    return pad + _yaml_scalar(v) + "\n"
+
+
+def _yaml_scalar(x) -> str:
+    if isinstance(x, (list, tuple)):
+        return "[" + ", ".join(_yaml_scalar(y) for y in x) + "]"
+    if isinstance(x, bool):
+        return "true" if x else "false"
+    if isinstance(x, (int, np.integer)):
+        return str(int(x))
+    if isinstance(x, (float, np.floating)):
+        return repr(float(x))
+    return str(x)
+
+
+def write_scene(desc: SceneDesc, directory: str | os.PathLike, name: str = "scene.yml") -> Path:
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    lines = ["version: 5", "scene:", "  primitives:"]
+    for i, p in enumerate(desc.primitives):
+        lines.append(f"    - type: [{', '.join(p.type)}]")
+        if p.mesh is not None:
+            fn = f"{i:04d}_{p.name}.obj"
+            write_obj(d / fn, p.mesh, p.name)
+            lines.append("      mesh:")
+            lines.append(f"        path: '{fn}'")
+        lines.append("      params:")
+        lines.append(_yaml_value(p.params, 8).rstrip("\n"))
+        lines.append("")
+    path = d / name
+    path.write_text("\n".join(lines) + "\n")
+    return path
+
+
+WORKLOADS = {
+    "cornell_box": cornell_box,
+    "terrain_scene": terrain_scene,
+}
+
+
+def material_box(with_point=True, with_directional=True, level=2) -> SceneDesc:
+    """Cornell box holding one sphere of every BSDF (G, S reflection / refraction / fresnel)
+    plus, optionally, a point light and a directional light: covers every emitter and BSDF
+    branch of the path tracers in a few thousand triangles."""
+    s = cornell_box()
+    cam = s.primitives.pop()  # keep the camera last
+    spheres = [
+        ((0.25, 0.75, 0.5), 0.12, glossy((0.9, 0.8, 0.7), 0.2)),
+        ((0.75, 0.75, 0.5), 0.12, mirror((0.9, 0.9, 0.9))),
+        ((0.5, 0.45, 0.8), 0.1, (["S"], {"S": {"type": "refraction", "refraction": {"R": [1.0, 1.0, 1.0],
+                                                                                      "eta1": 1.0, "eta2": 1.33}}})),
+        ((0.5, 0.8, 0.75), 0.09, glass(1.5)),
+    ]
+    for i, (c, r, (t, p)) in enumerate(spheres):
+        s.primitives.append(Primitive(t, p, sphere_mesh(c, r, level), f"ball{i}"))
+    if with_point:
+        s.primitives.append(Primitive(["L"], {"L": {"type": "point", "point": {"Le": [0.3, 0.3, 0.3],
+                                                                              "position": [0.5, 0.9, 0.6]}}},
+                                      None, "pointlight"))
+    if with_directional:
+        s.primitives.append(Primitive(["L"], {"L": {"type": "directional", "directional": {
+            "Le": [1.0, 1.0, 1.0], "direction": [0.0, -1.0, 0.0]}}}, None, "sun"))
+    s.primitives.append(cam)
+    return s
+
+
+def area_sensor_box() -> SceneDesc:
+    """Cornell box seen through an area sensor: a quad with uvs just inside the open face,
+    facing into the box (EType::Area, rt.hpp:1910-1929)."""
+    s = cornell_box()
+    s.primitives.pop()  # drop the pinhole
+    m = quad((0.05, 0.05, 0.999), (0.05, 0.95, 0.999), (0.95, 0.95, 0.999), (0.05 + 0.9, 0.05, 0.999), (0, 0, -1))
+    # uv = raster position: u along +x, v along +y
+    m.uvs = _f32([[0, 0], [0, 1], [1, 1], [1, 0]])
+    s.primitives.append(Primitive(["E"], {"E": {"type": "area", "area": {"We": [1.0, 1.0, 1.0]}}}, m, "sensor"))
+    return s
+
+
+def sphere_field(num_spheres=40, grid=96, level=3, seed=11) -> SceneDesc:
+    """A small terrain_scene (same generator, fewer triangles) for traversal tests."""
+    s = terrain_scene(num_spheres=num_spheres, grid=grid, level=level, seed_terrain=seed, seed_spheres=seed + 1)
+    return s
+
+
+WORKLOADS.update({"material_box": material_box, "area_sensor_box": area_sensor_box, "sphere_field": sphere_field})
