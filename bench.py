@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 `ptdirect` path tracer on the ~1.55 M-triangle terrain workload.
+
+Workload: procedural 512 x 512 fBm terrain + 200 level-4 icospheres (diffuse / glossy /
+mirror / glass) + 4 quad lights, 1920 x 1080, max path length 16, `ptdirect` (the
+configuration the headline metric is quoted on). A step renders `--spp-per-step` samples
+per pixel of the full frame; the default 16 steps x 16 spp make the configuration's 256 spp.
+
+Reported (one JSON line on rank 0):
+  value      Mrays/s (extension rays, camera rays included, + shadow rays) over the timed
+             steps, inputs resident in HBM, film accumulated on the device
+  e2e        the same metric through the C ABI's host-buffer entry point ngi_render: params
+             in, normalised film copied to pinned host memory every step
+  roofline   the dominant traversal kernel's algorithmic bytes per launch / its CUDA-event
+             duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (the reference's algorithm restated, FP64, mt19937 stream)
+             on this host's cores over a bounded sample of the same workload
+`--impl reference` times that CPU implementation alone, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s & time to rel-RMSE 1% vs FP64 ref: tuned vs plain GPU pt; grad/fwd cost"
+WIDTH, HEIGHT, MAX_VERTICES, RENDERER = 1920, 1080, 16, "ptdirect"
+L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp-per-step", type=int, default=16)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scene-dir", default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(scene_dir: str | None):
+    from nanogi_gb300 import scenegen
+
+    desc = scenegen.terrain_scene()
+    d = Path(scene_dir) if scene_dir else Path(tempfile.mkdtemp(prefix="ngi_terrain_"))
+    path = d / "scene.yml"
+    if not path.exists():
+        scenegen.write_scene(desc, d)
+    return desc, path
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "roofline_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_baseline(desc, spp_rays_hint, seconds, threads=0):
+    """Times the oracle (reference algorithm, FP64, mt19937 stream) on this host."""
+    from oracle.oracle import OracleScene
+
+    ora = OracleScene.from_desc(desc, WIDTH / HEIGHT)
+    n0 = 20000
+    ora.render(RENDERER, num_samples=n0, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=1,
+               rng_mode="reference", threads=threads, grain=1000)
+    st = ora.last_stats
+    n = int(max(n0, min(n0 * seconds / max(st["seconds"], 1e-3), 2e8)))
+    ora.render(RENDERER, num_samples=n, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=2,
+               rng_mode="reference", threads=threads, grain=10000)
+    st = ora.last_stats
+    rays = st["extension_rays"] + st["shadow_rays"]
+    return {"value": rays / st["seconds"] / 1e6, "unit": "Mrays/s", "cores": int(st["threads"]), "kind": "port",
+            "sample": f"{n} samples of the {WIDTH}x{HEIGHT} {RENDERER} frame ({rays} rays, {st['seconds']:.1f} s)",
+            "msamples_per_s": n / st["seconds"] / 1e6}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    desc = __import__("nanogi_gb300.scenegen", fromlist=["x"]).terrain_scene()
+    from oracle.oracle import OracleScene
+
+    ora = OracleScene.from_desc(desc, WIDTH / HEIGHT)
+    n_step = int(os.environ.get("NGI_REF_SAMPLES_PER_STEP", "100000"))
+    for i in range(args.warmup):
+        ora.render(RENDERER, num_samples=n_step // 4, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT,
+                   seed=100 + i, rng_mode="reference", grain=1000)
+    rays = 0
+    secs = 0.0
+    threads = 0
+    for i in range(args.steps):
+        ora.render(RENDERER, num_samples=n_step, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=200 + i,
+                   rng_mode="reference", grain=1000, sample_offset=i * n_step)
+        st = ora.last_stats
+        rays += st["extension_rays"] + st["shadow_rays"]
+        secs += st["seconds"]
+        threads = st["threads"]
+    value = rays / secs / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"terrain_scene 1.55M tris, {WIDTH}x{HEIGHT}, {RENDERER}, max length {MAX_VERTICES}",
+                   "samples_per_step": n_step},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} x {n_step} samples of the {WIDTH}x{HEIGHT} frame"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import capi
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    desc, path = make_scene(args.scene_dir)
+    scene = ng.Scene.load(path, WIDTH / HEIGHT)
+    scene.build()
+    info = scene.info()
+
+    spp = args.spp_per_step
+    n_step = WIDTH * HEIGHT * spp
+    film = torch.zeros((HEIGHT, WIDTH, 3), dtype=torch.float64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    # One dedicated stream: the render kernels, the L2 flush and the timing events all run on it.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+
+    def render_step(offset, flags=0):
+        r = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
+                        height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags)
+        r.render_device(scene, film.data_ptr(), stream.cuda_stream)
+        return r.last_stats
+
+    # rank r renders its own sample range: weak scaling, no data-path collective
+    base = rank * (args.warmup + args.steps) * n_step
+    for i in range(args.warmup):
+        flush.zero_()
+        render_step(base + i * n_step)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    totals = dict(rays=0, samples=0, launches=0)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for i in range(args.steps):
+            flush.zero_()
+            st = render_step(base + (args.warmup + i) * n_step)
+            totals["rays"] += st["extension_rays"] + st["shadow_rays"]
+            totals["samples"] += st["camera_rays"]
+            totals["launches"] += 3 * st["iterations"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms, totals["rays"], totals["samples"]], dtype=torch.float64, device=dev)
+        mx = t[:1].clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        ms = float(mx.item())
+        all_rays, all_samples = float(t[1].item()), float(t[2].item())
+        # one film exchange per job: sum of every rank's samples (outside the timed region)
+        torch.distributed.all_reduce(film)
+    else:
+        all_rays, all_samples = float(totals["rays"]), float(totals["samples"])
+    value = all_rays / (ms / 1e3) / 1e6
+
+    # ---- per-kernel timing and traversal counters (separate, untimed renders) ----
+    st_t = render_step(base, flags=capi.KERNEL_TIMING)
+    st_c = render_step(base, flags=capi.TRAVERSAL_COUNTERS)
+    kern = {"k_logic": st_t["logic_ms"], "k_extend": st_t["extend_ms"], "k_shadow": st_t["shadow_ms"]}
+    top = max(["k_extend", "k_shadow"], key=lambda k: kern[k])
+    launches = st_t["extend_launches"]
+    if top == "k_extend":
+        rays_k, nodes, tris, out_b = st_c["extension_rays"], st_c["extend_nodes"], st_c["extend_tris"], 16
+    else:
+        rays_k, nodes, tris, out_b = st_c["shadow_rays"], st_c["shadow_nodes"], st_c["shadow_tris"], 4
+    alg_bytes = rays_k * (32 + out_b) + 80 * nodes + 48 * tris
+    per_launch_bytes = alg_bytes / max(launches, 1)
+    per_launch_ms = kern[top] / max(launches, 1)
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = ncu_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None, "kernel": top,
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
+                "avg_launch_ms": per_launch_ms, "nodes_per_ray": nodes / max(rays_k, 1),
+                "tris_per_ray": tris / max(rays_k, 1),
+                "kernel_ms_share": {k: v / max(sum(kern.values()), 1e-9) for k, v in kern.items()}}
+
+    # ---- end to end through the host-buffer C ABI entry point ----
+    host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
+    r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
+                        height=HEIGHT, seed=99 + rank, precision=args.precision)
+    r_e2e.render(scene, host_film)  # warm the host-film path
+    torch.cuda.synchronize()
+    e_rays = 0
+    t0 = time.perf_counter()
+    for i in range(args.e2e_steps):
+        r_e2e.sample_offset = (i + 1) * n_step
+        r_e2e.render(scene, host_film)
+        e_rays += r_e2e.last_stats["extension_rays"] + r_e2e.last_stats["shadow_rays"]
+    e_sec = time.perf_counter() - t0
+    e2e = {"value": e_rays / e_sec / 1e6, "unit": "Mrays/s",
+           "h2d_bytes_per_step": ctypes_sizeof_params(), "d2h_bytes_per_step": WIDTH * HEIGHT * 3 * 8,
+           "steps": args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(desc, None, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": {"workload": f"terrain_scene: 512x512 fBm terrain + 200 level-4 icospheres + 4 quad lights, "
+                                   f"{info['num_triangles']} tris, {WIDTH}x{HEIGHT}, {RENDERER}, max length "
+                                   f"{MAX_VERTICES}, {spp} spp per step", "spp_total": spp * args.steps,
+                       "precision": f"{args.precision} shading, fp64 film", "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{world}, disjoint sample ranges"},
+            "msamples_per_s": all_samples / (ms / 1e3) / 1e6,
+            "rays_per_sample": all_rays / max(all_samples, 1),
+            "bvh_build_ms": info["bvh_build_ms"], "bvh_bytes": info["bvh_bytes"],
+            "roofline": roofline, "e2e": e2e, "gpu_launches": totals["launches"], "clocks": clocks.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    scene.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_sizeof_params():
+    import ctypes
+
+    from nanogi_gb300.capi import RenderParams
+
+    return ctypes.sizeof(RenderParams)
+
+
+if __name__ == "__main__":
+    main()

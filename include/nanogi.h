@@ -81,7 +81,13 @@ typedef struct ngi_render_params {
     int32_t raster_mode;       /* ngi_raster_mode */
     int32_t wave_size;         /* path slots resident on the device; 0 = auto */
     int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
+    int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
 } ngi_render_params;
+
+/* Measurement flags (results in ngi_render_stats). Both change only how the render is
+ * launched or instrumented, never its result. */
+#define NGI_RENDER_KERNEL_TIMING 1        /* launch without graphs, CUDA events around each kernel */
+#define NGI_RENDER_TRAVERSAL_COUNTERS 2   /* count BVH nodes and triangles visited per ray */
 
 /* Counters of the last render on a scene handle (per-stage ray counts etc). */
 typedef struct ngi_render_stats {
@@ -91,7 +97,12 @@ typedef struct ngi_render_stats {
     int64_t film_contributions;/* non-zero contributions added to the film */
     int64_t iterations;        /* wave iterations executed */
     int64_t nonfinite;         /* NaN/Inf contributions dropped (reported, never trapped) */
-    double render_ms;          /* device time of the render (CUDA events on the scene stream) */
+    double render_ms;          /* device time of the render (CUDA events on the render stream) */
+    /* NGI_RENDER_KERNEL_TIMING: summed device time and launch count per kernel */
+    double logic_ms, extend_ms, shadow_ms;
+    int64_t logic_launches, extend_launches, shadow_launches;
+    /* NGI_RENDER_TRAVERSAL_COUNTERS: nodes / triangles visited, over all rays of each kind */
+    int64_t extend_nodes, extend_tris, shadow_nodes, shadow_tris;
 } ngi_render_stats;
 
 /* Scene summary (host side; available without a GPU). */
@@ -129,6 +140,12 @@ NGI_API ngi_status ngi_scene_load(const char* yaml_path, double aspect, ngi_scen
 NGI_API void ngi_scene_free(ngi_scene* scene);
 
 NGI_API ngi_status ngi_scene_get_info(const ngi_scene* scene, ngi_scene_info* out_info);
+
+/* Copies the flattened host triangle arrays (what Scene::Load produced, rt.hpp:1676-1731):
+ * pos/nrm: num_triangles*9 floats (p1,p2,p3 / n1,n2,n3), uv: num_triangles*6 floats (zeros
+ * when the mesh has none), prim: owning primitive per triangle. Any pointer may be NULL.
+ * Host only; no GPU needed. */
+NGI_API ngi_status ngi_scene_get_triangles(const ngi_scene* scene, float* pos, float* nrm, float* uv, int32_t* prim);
 
 /* Uploads the flattened scene and builds the compressed 8-wide BVH on the GPU: the
  * counterpart of the Embree build in include/nanogi/rt.hpp:2087-2143. Called implicitly

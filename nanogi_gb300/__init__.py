@@ -72,6 +72,16 @@ class Scene:
         d["bound_max"] = list(inf.bound_max)
         return d
 
+    def triangles(self):
+        """Flattened host arrays: pos (n,3,3), nrm (n,3,3), uv (n,3,2) float32, prim (n,) int32."""
+        n = self.info()["num_triangles"]
+        pos = np.empty((n, 3, 3), np.float32)
+        nrm = np.empty((n, 3, 3), np.float32)
+        uv = np.empty((n, 3, 2), np.float32)
+        prim = np.empty(n, np.int32)
+        check(load_library().ngi_scene_get_triangles(self.handle, _ptr(pos), _ptr(nrm), _ptr(uv), _ptr(prim)))
+        return pos, nrm, uv, prim
+
     def build(self) -> None:
         check(load_library().ngi_scene_build(self.handle))
 
@@ -113,6 +123,7 @@ class Renderer:
     raster: str = "stratified"
     wave_size: int = 0
     iterations_per_graph: int = 0
+    flags: int = 0
     last_stats: dict = field(default_factory=dict, repr=False)
 
     def params(self) -> RenderParams:
@@ -130,6 +141,7 @@ class Renderer:
             raster_mode=capi.RASTER_MODES[self.raster],
             wave_size=int(self.wave_size),
             iterations_per_graph=int(self.iterations_per_graph),
+            flags=int(self.flags),
         )
 
     def render(self, scene: Scene, film: np.ndarray | None = None) -> np.ndarray:

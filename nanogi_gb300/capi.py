@@ -41,7 +41,12 @@ class RenderParams(ctypes.Structure):
         ("raster_mode", ctypes.c_int32),
         ("wave_size", ctypes.c_int32),
         ("iterations_per_graph", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
     ]
+
+
+KERNEL_TIMING = 1
+TRAVERSAL_COUNTERS = 2
 
 
 class RenderStats(ctypes.Structure):
@@ -53,6 +58,16 @@ class RenderStats(ctypes.Structure):
         ("iterations", ctypes.c_int64),
         ("nonfinite", ctypes.c_int64),
         ("render_ms", ctypes.c_double),
+        ("logic_ms", ctypes.c_double),
+        ("extend_ms", ctypes.c_double),
+        ("shadow_ms", ctypes.c_double),
+        ("logic_launches", ctypes.c_int64),
+        ("extend_launches", ctypes.c_int64),
+        ("shadow_launches", ctypes.c_int64),
+        ("extend_nodes", ctypes.c_int64),
+        ("extend_tris", ctypes.c_int64),
+        ("shadow_nodes", ctypes.c_int64),
+        ("shadow_tris", ctypes.c_int64),
     ]
 
 
@@ -81,6 +96,8 @@ PROTOTYPES = {
     "ngi_scene_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, _P(ctypes.c_void_p)]),
     "ngi_scene_free": (None, [ctypes.c_void_p]),
     "ngi_scene_get_info": (ctypes.c_int, [ctypes.c_void_p, _P(SceneInfo)]),
+    "ngi_scene_get_triangles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "ngi_scene_build": (ctypes.c_int, [ctypes.c_void_p]),
     "ngi_render": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p]),
     "ngi_render_device": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p, ctypes.c_void_p]),

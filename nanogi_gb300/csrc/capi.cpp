@@ -124,6 +124,17 @@ NGI_API ngi_status ngi_scene_get_info(const ngi_scene* scene, ngi_scene_info* ou
     return NGI_OK;
 }
 
+NGI_API ngi_status ngi_scene_get_triangles(const ngi_scene* scene, float* pos, float* nrm, float* uv, int32_t* prim) {
+    if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
+    const ngi::HostScene& h = *scene->host;
+    if (pos && !h.tri_pos.empty()) std::memcpy(pos, h.tri_pos.data(), h.tri_pos.size() * sizeof(float));
+    if (nrm && !h.tri_nrm.empty()) std::memcpy(nrm, h.tri_nrm.data(), h.tri_nrm.size() * sizeof(float));
+    if (uv && !h.tri_uv.empty()) std::memcpy(uv, h.tri_uv.data(), h.tri_uv.size() * sizeof(float));
+    if (prim && !h.tri_prim.empty()) std::memcpy(prim, h.tri_prim.data(), h.tri_prim.size() * sizeof(int32_t));
+    g_last_error.clear();
+    return NGI_OK;
+}
+
 NGI_API ngi_status ngi_scene_build(ngi_scene* scene) {
     if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
     return Guard([&]() {

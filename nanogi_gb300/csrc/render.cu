@@ -49,6 +49,7 @@ struct WaveCounters {
     unsigned long long stat_shadow;
     unsigned long long stat_contrib;
     unsigned long long stat_nonfinite;
+    unsigned long long ext_nodes, ext_tris, sh_nodes, sh_tris;  // traversal counters
 };
 
 struct RenderConsts {
@@ -421,31 +422,45 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
     }
 }
 
-template <typename R>
+// Adds a per-thread traversal count into a global counter with one atomic per warp.
+NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+    if (lane_id() == 0 && x) atomicAdd(counter, x);
+}
+
+template <typename R, bool STATS>
 __global__ void __launch_bounds__(256) k_extend(SceneView<R> sv, WaveView<R> w) {
     const int n = w.ctr->ext_count;
     bool overflow = false;
+    TraceStats ts{0u, 0u};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int s = w.ext_queue[i];
         const float4 o = w.ray_o[s], d = w.ray_d[s];
         float tmax = d.w, u = 0.0f, v = 0.0f;
-        const int ti = trace_ray<false, false>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
-                                               tmax, u, v, overflow, nullptr);
+        const int ti = trace_ray<false, STATS>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
+                                               tmax, u, v, overflow, &ts);
         w.hit[s] = make_float4(tmax, u, v, __int_as_float(ti));
     }
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    if (STATS) {
+        warp_sum_add(&w.ctr->ext_nodes, ts.nodes);
+        warp_sum_add(&w.ctr->ext_tris, ts.tris);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_ext, (unsigned long long)n);
 }
 
-template <typename R>
+template <typename R, bool STATS>
 __global__ void __launch_bounds__(256) k_shadow(SceneView<R> sv, WaveView<R> w) {
     const int n = w.ctr->sh_count;
     bool overflow = false;
+    TraceStats ts{0u, 0u};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 o = w.sh_o[i], d = w.sh_d[i];
         float tmax = d.w, u, v;
-        const int ti = trace_ray<true, false>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
-                                              tmax, u, v, overflow, nullptr);
+        const int ti = trace_ray<true, STATS>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
+                                              tmax, u, v, overflow, &ts);
         if (ti < 0) {
             const Vec4T<R> c = w.sh_c[i];
             const V3<R> cc = v3<R>(c.x, c.y, c.z);
@@ -458,6 +473,10 @@ __global__ void __launch_bounds__(256) k_shadow(SceneView<R> sv, WaveView<R> w) 
         }
     }
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    if (STATS) {
+        warp_sum_add(&w.ctr->sh_nodes, ts.nodes);
+        warp_sum_add(&w.ctr->sh_tris, ts.tris);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_shadow, (unsigned long long)n);
 }
 
@@ -743,37 +762,50 @@ int grid_for(int items, int block) {
     return std::max(1, std::min(max_blocks, (items + block - 1) / block));
 }
 
-template <typename R, bool DIRECT>
+template <typename R, bool DIRECT, bool STATS>
+void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
+                       int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev) {
+    const size_t off = offsetof(WaveCounters, ext_count);
+    const size_t len = offsetof(WaveCounters, error_flags) - off;
+    cudaMemsetAsync((char*)ctr + off, 0, len, stream);
+    if (ev) cudaEventRecord(ev[0], stream);
+    k_logic<R, DIRECT><<<g_logic, 256, 0, stream>>>(sv, v, rc);
+    if (ev) cudaEventRecord(ev[1], stream);
+    k_extend<R, STATS><<<g_trace, 256, 0, stream>>>(sv, v);
+    if (ev) cudaEventRecord(ev[2], stream);
+    k_shadow<R, STATS><<<g_trace, 256, 0, stream>>>(sv, v);
+    if (ev) cudaEventRecord(ev[3], stream);
+}
+
+template <typename R, bool DIRECT, bool STATS>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
-              cudaStream_t stream) {
+              bool kernel_timing, cudaStream_t stream) {
     DeviceScene& ds = *hs.dev;
     const SceneView<R> sv = make_view<R>(ds);
-    const int block = 256;
-    const int g_logic = grid_for(v.Q, block);
-    const int g_trace = grid_for(2 * v.Q, block);
-    const size_t ctr_reset_off = offsetof(WaveCounters, ext_count);
-    const size_t ctr_reset_len = offsetof(WaveCounters, error_flags) - ctr_reset_off;
+    const int g_logic = grid_for(v.Q, 256);
+    const int g_trace = grid_for(2 * v.Q, 256);
 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
 
-    cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < iters_per_graph; it++) {
-        cudaMemsetAsync((char*)wv->ctr + ctr_reset_off, 0, ctr_reset_len, stream);
-        k_logic<R, DIRECT><<<g_logic, block, 0, stream>>>(sv, v, rc);
-        k_extend<R><<<g_trace, block, 0, stream>>>(sv, v);
-        k_shadow<R><<<g_trace, block, 0, stream>>>(sv, v);
+    if (!kernel_timing) {
+        cudaGraph_t graph = nullptr;
+        CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < iters_per_graph; it++)
+            enqueue_iteration<R, DIRECT, STATS>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr);
+        const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
+        if (cap != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            throw DeviceError(std::string("graph capture failed: ") + cudaGetErrorString(cap));
+        }
+        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
     }
-    const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
-    if (cap != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        throw DeviceError(std::string("graph capture failed: ") + cudaGetErrorString(cap));
-    }
-    const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
+    cudaEvent_t kev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double kms[3] = {0, 0, 0};
+    long long launches = 0;
 
     long long iterations = 0;
     // Each path ends within (max vertices) iterations after it starts; the bound below is
@@ -781,10 +813,25 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
     const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
     try {
+        if (kernel_timing)
+            for (auto& e : kev) CUDA_CHECK(cudaEventCreate(&e));
         CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
         while (true) {
-            CUDA_CHECK(cudaGraphLaunch(exec, stream));
-            iterations += iters_per_graph;
+            if (kernel_timing) {
+                enqueue_iteration<R, DIRECT, STATS>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev);
+                CUDA_CHECK(cudaGetLastError());
+                CUDA_CHECK(cudaEventSynchronize(kev[3]));
+                for (int k = 0; k < 3; k++) {
+                    float t = 0;
+                    CUDA_CHECK(cudaEventElapsedTime(&t, kev[k], kev[k + 1]));
+                    kms[k] += t;
+                }
+                launches++;
+                iterations++;
+            } else {
+                CUDA_CHECK(cudaGraphLaunch(exec, stream));
+                iterations += iters_per_graph;
+            }
             CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, stream));
             CUDA_CHECK(cudaStreamSynchronize(stream));
             if (wv->h_ctr->error_flags & 1)
@@ -796,13 +843,25 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         CUDA_CHECK(cudaEventSynchronize(wv->ev1));
     } catch (...) {
         cudaStreamSynchronize(stream);
-        cudaGraphExecDestroy(exec);
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto& e : kev)
+            if (e) cudaEventDestroy(e);
         throw;
     }
-    cudaGraphExecDestroy(exec);
+    if (exec) cudaGraphExecDestroy(exec);
+    for (auto& e : kev)
+        if (e) cudaEventDestroy(e);
     float ms = 0;
     cudaEventElapsedTime(&ms, wv->ev0, wv->ev1);
     const WaveCounters& c = *wv->h_ctr;
+    ds.last_stats.logic_ms = kms[0];
+    ds.last_stats.extend_ms = kms[1];
+    ds.last_stats.shadow_ms = kms[2];
+    ds.last_stats.logic_launches = ds.last_stats.extend_launches = ds.last_stats.shadow_launches = launches;
+    ds.last_stats.extend_nodes = (int64_t)c.ext_nodes;
+    ds.last_stats.extend_tris = (int64_t)c.ext_tris;
+    ds.last_stats.shadow_nodes = (int64_t)c.sh_nodes;
+    ds.last_stats.shadow_tris = (int64_t)c.sh_tris;
     ds.last_stats.camera_rays = (int64_t)c.stat_camera;
     ds.last_stats.extension_rays = (int64_t)c.stat_ext;
     ds.last_stats.shadow_rays = (int64_t)c.stat_shadow;
@@ -841,16 +900,24 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
+    const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
+    const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
+    const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
     if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v = wv->vd;
         v.film = d_film;
-        if (p.renderer == NGI_RENDERER_PTDIRECT) run_wave<double, true>(hs, wv, v, rc, ipg, stream);
-        else run_wave<double, false>(hs, wv, v, rc, ipg, stream);
+        if (direct) run_wave<double, true, false>(hs, wv, v, rc, ipg, timing, stream);
+        else run_wave<double, false, false>(hs, wv, v, rc, ipg, timing, stream);
     } else {
         WaveView<float> v = wv->vf;
         v.film = d_film;
-        if (p.renderer == NGI_RENDERER_PTDIRECT) run_wave<float, true>(hs, wv, v, rc, ipg, stream);
-        else run_wave<float, false>(hs, wv, v, rc, ipg, stream);
+        if (direct) {
+            if (counters) run_wave<float, true, true>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<float, true, false>(hs, wv, v, rc, ipg, timing, stream);
+        } else {
+            if (counters) run_wave<float, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<float, false, false>(hs, wv, v, rc, ipg, timing, stream);
+        }
     }
 }
 

@@ -37,8 +37,11 @@ def _check_hits(gpu, ora, label):
     assert miss_agree.mean() > 0.9999, f"{label}: hit/miss disagree on {(~miss_agree).sum()} rays"
     both = (gp >= 0) & (op >= 0)
     same = gp[both] == op[both]
-    # ties (two triangles at the same distance) may resolve differently; they are rare
-    assert same.mean() > 0.9999, f"{label}: {(~same).sum()} of {both.sum()} primitive ids differ"
+    # A different primitive is only allowed for a tie: two triangles at the very same
+    # distance (e.g. coplanar faces), where traversal order picks one of them.
+    tie = ~same
+    assert np.array_equal(gt[both][tie], ot[both][tie]), f"{label}: primitive ids differ on non-tie rays"
+    assert tie.mean() < 0.01, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
     rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
     assert rel.max() <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
     exact = (gt[both][same] == ot[both][same]).mean()
