@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scene-dir", default=None)
+    ap.add_argument("--wave-size", type=int, default=0, help="path slots (0 = library default)")
     return ap.parse_args()
 
 
@@ -152,11 +153,16 @@ def cpu_baseline(desc, spp_rays_hint, seconds, threads=0):
     from oracle.oracle import OracleScene
 
     ora = OracleScene.from_desc(desc, WIDTH / HEIGHT)
-    n0 = 20000
-    ora.render(RENDERER, num_samples=n0, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=1,
-               rng_mode="reference", threads=threads, grain=1000)
-    st = ora.last_stats
-    n = int(max(n0, min(n0 * seconds / max(st["seconds"], 1e-3), 2e8)))
+    # Calibrate: every render pays a fixed cost (per-thread W*H films, as the reference's
+    # Context::film does) plus a per-sample cost; size the timed sample to ~`seconds`.
+    times = []
+    for n_cal in (100_000, 400_000):
+        ora.render(RENDERER, num_samples=n_cal, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=1,
+                   rng_mode="reference", threads=threads, grain=1000)
+        times.append(ora.last_stats["seconds"])
+    per_sample = max((times[1] - times[0]) / 300_000, 1e-9)
+    fixed = max(times[0] - 100_000 * per_sample, 0.0)
+    n = int(min(max((seconds - fixed) / per_sample, 400_000), 2e9))
     ora.render(RENDERER, num_samples=n, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT, seed=2,
                rng_mode="reference", threads=threads, grain=10000)
     st = ora.last_stats
@@ -229,13 +235,15 @@ def main():
     n_step = WIDTH * HEIGHT * spp
     film = torch.zeros((HEIGHT, WIDTH, 3), dtype=torch.float64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()  # the zero-fills above must land before the render stream uses them
     # One dedicated stream: the render kernels, the L2 flush and the timing events all run on it.
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
     def render_step(offset, flags=0):
         r = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
-                        height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags)
+                        height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags,
+                        wave_size=args.wave_size)
         r.render_device(scene, film.data_ptr(), stream.cuda_stream)
         return r.last_stats
 
@@ -300,7 +308,7 @@ def main():
     # ---- end to end through the host-buffer C ABI entry point ----
     host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
     r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
-                        height=HEIGHT, seed=99 + rank, precision=args.precision)
+                        height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size)
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0
