@@ -138,13 +138,14 @@ def measured_peak():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "roofline_traffic.json"
+    """Per-launch DRAM bytes of k_extend from the committed ncu summary, if any."""
+    import re
+
+    p = ROOT / "profiles" / "k_extend_terrain_small.md"
     if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except ValueError:
-            return None
+        m = re.search(r"^dram_bytes_per_launch:\s*(\d+)", p.read_text(), re.M)
+        if m:
+            return {"dram_bytes_per_launch": int(m.group(1))}
     return None
 
 
