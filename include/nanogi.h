@@ -168,6 +168,29 @@ NGI_API ngi_status ngi_render_device(ngi_scene* scene, const ngi_render_params* 
 
 NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats* out_stats);
 
+/* Allocation-free variant of ngi_render_device. It has no counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory while they render: an application whose
+ * own allocator owns the whole device, a real-time loop that cannot take the device-wide
+ * synchronisation cudaMalloc / cudaFree may cause, or a process held to a fixed memory
+ * budget. The call allocates nothing (no cudaMalloc, cudaFree, graph or event creation):
+ * the render's scratch -- its wave of path slots, queues and counters -- lives in one
+ * 32 MiB file-scope device array that every GPU loading this library holds until exit.
+ *
+ * Limits and rules:
+ *   - the scene must already be on the device (ngi_scene_build), else NGI_ERR_INVALID_ARGUMENT;
+ *   - params->wave_size must be 0 (= 65536) or at most 65536 path slots, else
+ *     NGI_ERR_INVALID_ARGUMENT; num_samples is not bounded (samples stream through the wave);
+ *   - params->flags must be 0;
+ *   - the caller passes the output: d_film_rgb, a DEVICE array of width*height*3 doubles that
+ *     receives the raw sums added to its contents, as with ngi_render_device;
+ *   - the first call on each device looks up the array's device address (with that device
+ *     current); make that first call before any stream capture;
+ *   - every call shares the array and clears what must start at zero; calls that overlap on
+ *     the GPU (e.g. from two streams at once) race on it and must not be made. */
+NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_params* params,
+                                             double* d_film_rgb, void* stream);
+
 /* ---- parity hooks ------------------------------------------------------------------ */
 
 /* Scene::Intersect(ray, isect, minT, maxT)  include/nanogi/rt.hpp:2162-2244, restricted

@@ -102,6 +102,8 @@ PROTOTYPES = {
     "ngi_render": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p]),
     "ngi_render_device": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_get_render_stats": (ctypes.c_int, [ctypes.c_void_p, _P(RenderStats)]),
+    "ngi_render_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p,
+                                                 ctypes.c_void_p]),
     "ngi_intersect": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_visible": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

@@ -164,6 +164,17 @@ NGI_API ngi_status ngi_render_device(ngi_scene* scene, const ngi_render_params* 
     });
 }
 
+NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_params* params, double* d_film_rgb,
+                                             void* stream) {
+    const ngi_status st = CheckParams(scene, params);
+    if (st != NGI_OK) return st;
+    if (!d_film_rgb) return Fail(NGI_ERR_INVALID_ARGUMENT, "film is NULL");
+    return Guard([&]() {
+        ngi::DeviceRenderNoAlloc(*scene->host, *params, d_film_rgb, (cudaStream_t)stream);
+        return NGI_OK;
+    });
+}
+
 NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats* out) {
     if (!scene || !scene->host || !out) return Fail(NGI_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!scene->host->dev) {

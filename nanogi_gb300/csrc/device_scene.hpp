@@ -69,6 +69,10 @@ void DeviceRender(HostScene& scene, const ngi_render_params& params, double* d_f
 // device and copies the normalised film into host memory.
 void DeviceRenderToHost(HostScene& scene, const ngi_render_params& params, double* h_film);
 
+// Same render with all scratch in a fixed file-scope device array: allocates nothing.
+// Needs the scene built beforehand; bounds the wave at 65536 path slots.
+void DeviceRenderNoAlloc(HostScene& scene, const ngi_render_params& params, double* d_film, cudaStream_t stream);
+
 // Parity hooks.
 void DeviceIntersect(HostScene& scene, const float* h_rays, int64_t n, int32_t* prim, float* t, float* uv);
 void DeviceVisible(HostScene& scene, const double* h_points, int64_t n, uint8_t* visible);

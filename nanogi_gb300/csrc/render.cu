@@ -1018,4 +1018,163 @@ void DeviceVisible(HostScene& hs, const double* h_pts, int64_t n, uint8_t* vis) 
     cleanup();
 }
 
+// ---- allocation-free render --------------------------------------------------------------------
+// Some callers cannot allocate device memory at render time: an application whose own
+// allocator owns the whole device, a real-time loop that cannot afford the device-wide
+// synchronisation a cudaMalloc/cudaFree may cause, or a process working under a fixed
+// device-memory budget. For them the render's scratch (the wave of path slots, its queues
+// and counters) lives in one file-scope device array instead of per-call allocations.
+//
+// kNoAllocScratchBytes is the fixed size of that array; every GPU that loads this library
+// holds it until the process exits. It bounds the wave at kNoAllocMaxWave path slots (the
+// number of samples per call is not bounded: samples stream through the wave). All calls
+// share the array and it keeps the last call's contents, so each call clears its counters
+// and slot states first; two calls that overlap on the GPU (e.g. on two streams) race on it.
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
+constexpr int kNoAllocMaxWave = 1 << 16;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Carves the wave buffers of Q slots out of `base` (when non-null); returns the bytes used.
+template <typename R>
+size_t carve_wave(unsigned char* base, int Q, WaveView<R>& v) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> void* {
+        void* p = base ? (void*)(base + off) : nullptr;
+        off = align256(off + std::max<size_t>(bytes, 16));
+        return p;
+    };
+    v.Q = Q;
+    v.ctr = (WaveCounters*)take(sizeof(WaveCounters));
+    v.ray_o = (float4*)take(sizeof(float4) * Q);
+    v.ray_d = (float4*)take(sizeof(float4) * Q);
+    v.hit = (float4*)take(sizeof(float4) * Q);
+    v.thr = (Vec4T<R>*)take(sizeof(Vec4T<R>) * Q);
+    if (sizeof(R) == 8) {
+        v.od_o = (Vec4T<double>*)take(sizeof(Vec4T<double>) * Q);
+        v.od_d = (Vec4T<double>*)take(sizeof(Vec4T<double>) * Q);
+    } else {
+        v.od_o = v.od_d = nullptr;
+    }
+    v.pixel = (uint32_t*)take(sizeof(uint32_t) * Q);
+    v.sample = (unsigned long long*)take(sizeof(unsigned long long) * Q);
+    v.nverts = (int*)take(sizeof(int) * Q);
+    v.state = (uint8_t*)take(sizeof(uint8_t) * Q);
+    v.ext_queue = (int*)take(sizeof(int) * Q);
+    v.sh_o = (float4*)take(sizeof(float4) * 2 * (size_t)Q);
+    v.sh_d = (float4*)take(sizeof(float4) * 2 * (size_t)Q);
+    v.sh_c = (Vec4T<R>*)take(sizeof(Vec4T<R>) * 2 * (size_t)Q);
+    v.sh_pix = (uint32_t*)take(sizeof(uint32_t) * 2 * (size_t)Q);
+    return off;
+}
+
+// Device address of the scratch array, looked up once per device with that device current.
+unsigned char* noalloc_scratch_address() {
+    static unsigned char* addr[64] = {nullptr};
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw DeviceError("device ordinal out of range", NGI_ERR_INVALID_ARGUMENT);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            throw DeviceError(std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e));
+        addr[dev] = (unsigned char*)p;
+    }
+    return addr[dev];
+}
+
+template <typename R, bool DIRECT>
+void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, cudaStream_t stream) {
+    DeviceScene& ds = *hs.dev;
+    const SceneView<R> sv = make_view<R>(ds);
+    const int g_logic = grid_for(v.Q, 256);
+    const int g_trace = grid_for(2 * v.Q, 256);
+    CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
+    CUDA_CHECK(cudaMemsetAsync(v.ctr, 0, sizeof(WaveCounters), stream));
+    const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
+    const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
+    WaveCounters h{};
+    long long iterations = 0;
+    while (true) {
+        for (int k = 0; k < 4; k++)
+            enqueue_iteration<R, DIRECT, false>(sv, v, rc, v.ctr, g_logic, g_trace, stream, nullptr);
+        iterations += 4;
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(&h, v.ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        if (h.error_flags & 1) throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+        if (h.active == 0 && h.next_sample >= (unsigned long long)rc.num_samples) break;
+        if (iterations > max_iters) throw DeviceError("wave did not drain", NGI_ERR_DEVICE_TIMEOUT);
+    }
+    ds.last_stats = ngi_render_stats{};
+    ds.last_stats.camera_rays = (int64_t)h.stat_camera;
+    ds.last_stats.extension_rays = (int64_t)h.stat_ext;
+    ds.last_stats.shadow_rays = (int64_t)h.stat_shadow;
+    ds.last_stats.film_contributions = (int64_t)h.stat_contrib;
+    ds.last_stats.nonfinite = (int64_t)h.stat_nonfinite;
+    ds.last_stats.iterations = iterations;
+}
+
+}  // namespace
+
+void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_film, cudaStream_t user_stream) {
+    if (!hs.dev)
+        throw DeviceError("the scene is not on the device: call ngi_scene_build first (this entry point allocates "
+                          "nothing, so it cannot upload the scene)", NGI_ERR_INVALID_ARGUMENT);
+    DeviceScene& ds = *hs.dev;
+    if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
+    if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
+        throw DeviceError("ptdirect needs at least one light (the reference indexes an empty light list)",
+                          NGI_ERR_UNSUPPORTED);
+    if (p.flags != 0)
+        throw DeviceError("measurement flags are not available on the allocation-free entry point",
+                          NGI_ERR_INVALID_ARGUMENT);
+    if (p.wave_size > kNoAllocMaxWave)
+        throw DeviceError("wave_size " + std::to_string(p.wave_size) + " exceeds the allocation-free maximum of " +
+                              std::to_string(kNoAllocMaxWave) + " path slots",
+                          NGI_ERR_INVALID_ARGUMENT);
+    cudaStream_t stream = user_stream ? user_stream : ds.stream;
+    ds.last_stats = ngi_render_stats{};
+    if (p.num_samples == 0) return;
+    int Q = p.wave_size > 0 ? p.wave_size : kNoAllocMaxWave;
+    const long long need = std::max<long long>(p.num_samples, 256);
+    if ((long long)Q > need) Q = (int)need;
+    Q = (Q + 255) / 256 * 256;
+    unsigned char* base = noalloc_scratch_address();
+    RenderConsts rc{};
+    rc.renderer = p.renderer;
+    rc.max_vertices = p.max_num_vertices;
+    rc.num_samples = p.num_samples;
+    rc.sample_offset = p.sample_offset;
+    rc.seed = p.seed;
+    rc.width = p.width;
+    rc.height = p.height;
+    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
+    const long long wh = (long long)p.width * p.height;
+    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
+    if (p.precision == NGI_PRECISION_FP64) {
+        WaveView<double> v{};
+        if (carve_wave<double>(nullptr, Q, v) > kNoAllocScratchBytes)
+            throw DeviceError("allocation-free scratch too small for the wave", NGI_ERR_INVALID_ARGUMENT);
+        carve_wave<double>(base, Q, v);
+        v.film = d_film;
+        if (direct) run_wave_noalloc<double, true>(hs, v, rc, stream);
+        else run_wave_noalloc<double, false>(hs, v, rc, stream);
+    } else {
+        WaveView<float> v{};
+        if (carve_wave<float>(nullptr, Q, v) > kNoAllocScratchBytes)
+            throw DeviceError("allocation-free scratch too small for the wave", NGI_ERR_INVALID_ARGUMENT);
+        carve_wave<float>(base, Q, v);
+        v.film = d_film;
+        if (direct) run_wave_noalloc<float, true>(hs, v, rc, stream);
+        else run_wave_noalloc<float, false>(hs, v, rc, stream);
+    }
+}
+
 }  // namespace ngi
