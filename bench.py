@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scene-dir", default=None)
     ap.add_argument("--wave-size", type=int, default=0, help="path slots (0 = library default)")
+    ap.add_argument("--trace-refill", type=int, default=0, help="traversal refill threshold (0 = default)")
     return ap.parse_args()
 
 
@@ -244,7 +245,7 @@ def main():
     def render_step(offset, flags=0):
         r = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
                         height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags,
-                        wave_size=args.wave_size)
+                        wave_size=args.wave_size, trace_refill=args.trace_refill)
         r.render_device(scene, film.data_ptr(), stream.cuda_stream)
         return r.last_stats
 
@@ -286,10 +287,11 @@ def main():
     # ---- per-kernel timing and traversal counters (separate, untimed renders) ----
     st_t = render_step(base, flags=capi.KERNEL_TIMING)
     st_c = render_step(base, flags=capi.TRAVERSAL_COUNTERS)
-    kern = {"k_logic": st_t["logic_ms"], "k_extend": st_t["extend_ms"], "k_shadow": st_t["shadow_ms"]}
-    top = max(["k_extend", "k_shadow"], key=lambda k: kern[k])
+    kern = {"k_logic": st_t["logic_ms"], "k_trace<extension>": st_t["extend_ms"],
+            "k_trace<shadow>": st_t["shadow_ms"]}
+    top = max(["k_trace<extension>", "k_trace<shadow>"], key=lambda k: kern[k])
     launches = st_t["extend_launches"]
-    if top == "k_extend":
+    if top == "k_trace<extension>":
         rays_k, nodes, tris, out_b = st_c["extension_rays"], st_c["extend_nodes"], st_c["extend_tris"], 16
     else:
         rays_k, nodes, tris, out_b = st_c["shadow_rays"], st_c["shadow_nodes"], st_c["shadow_tris"], 4
@@ -309,7 +311,8 @@ def main():
     # ---- end to end through the host-buffer C ABI entry point ----
     host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
     r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
-                        height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size)
+                        height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size,
+                        trace_refill=args.trace_refill)
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0

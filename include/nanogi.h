@@ -82,6 +82,7 @@ typedef struct ngi_render_params {
     int32_t wave_size;         /* path slots resident on the device; 0 = auto */
     int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
     int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
+    int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
 } ngi_render_params;
 
 /* Measurement flags (results in ngi_render_stats). Both change only how the render is

@@ -124,6 +124,7 @@ class Renderer:
     wave_size: int = 0
     iterations_per_graph: int = 0
     flags: int = 0
+    trace_refill: int = 0
     last_stats: dict = field(default_factory=dict, repr=False)
 
     def params(self) -> RenderParams:
@@ -142,6 +143,7 @@ class Renderer:
             wave_size=int(self.wave_size),
             iterations_per_graph=int(self.iterations_per_graph),
             flags=int(self.flags),
+            trace_refill=int(self.trace_refill),
         )
 
     def render(self, scene: Scene, film: np.ndarray | None = None) -> np.ndarray:

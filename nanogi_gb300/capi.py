@@ -42,6 +42,7 @@ class RenderParams(ctypes.Structure):
         ("wave_size", ctypes.c_int32),
         ("iterations_per_graph", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("trace_refill", ctypes.c_int32),
     ]
 
 

@@ -67,6 +67,8 @@ ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
         return Fail(NGI_ERR_INVALID_ARGUMENT, "raster_mode must be STRATIFIED or UNIFORM");
     if (p->wave_size < 0 || p->iterations_per_graph < 0 || p->iterations_per_graph > 64)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "wave_size / iterations_per_graph out of range");
+    if (p->trace_refill < 0 || p->trace_refill > 32)
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_refill must be 0 (auto) or 1..32");
     return NGI_OK;
 }
 

@@ -88,14 +88,48 @@ struct TraceStats {
     uint32_t tris;
 };
 
-NGI_D float byte_to_float(uint32_t word, int b) { return (float)((word >> (8 * b)) & 0xFFu); }
+// Byte b of a 32-bit word as an exact float: one byte permute builds the bit pattern of
+// 2^23 + byte, one subtraction removes the 2^23.
+NGI_D float byte_to_float(uint32_t word, int b) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)) - 8388608.0f;
+}
+
+// Per-ray state of one CWBVH traversal, kept in registers between steps so a warp can
+// interleave the rays of its lanes (and refill lanes whose ray has finished).
+struct TravState {
+    RayPre rp;
+    float idx, idy, idz;       // inverse direction (tiny components clamped) for the slab tests
+    uint32_t octinv;           // 7 - ray octant: traversal order of the children
+    uint32_t dneg;             // bit k set: direction component k is negative (near plane = hi)
+    float tmin, tmax;
+    float hu, hv;
+    int hit;
+    uint2 ngroup;              // node group: child base, internal-hit bits [31:24] | imask [7:0]
+    int sp;
+};
+
+NGI_D void trav_init(TravState& s, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
+                     float tmax) {
+    s.rp = ray_precompute(ox, oy, oz, dx, dy, dz);
+    const float kTiny = 1e-20f;
+    s.idx = __frcp_rn(fabsf(dx) > kTiny ? dx : copysignf(kTiny, dx));
+    s.idy = __frcp_rn(fabsf(dy) > kTiny ? dy : copysignf(kTiny, dy));
+    s.idz = __frcp_rn(fabsf(dz) > kTiny ? dz : copysignf(kTiny, dz));
+    const uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    s.octinv = 7u - oct;
+    s.dneg = (s.idx < 0.0f ? 1u : 0u) | (s.idy < 0.0f ? 2u : 0u) | (s.idz < 0.0f ? 4u : 0u);
+    s.tmin = tmin;
+    s.tmax = tmax;
+    s.hu = s.hv = 0.0f;
+    s.hit = -1;
+    s.ngroup = make_uint2(0u, 0x80000000u);  // the root as the only internal hit, imask 0
+    s.sp = 0;
+}
 
 // Intersects the 8 children of a node; returns the CWBVH hit mask
 // (bits 24..31: internal children by traversal priority, bits 0..23: leaf triangles).
-NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, float ox, float oy, float oz,
-                                  float idx_, float idy, float idz, uint32_t octinv,
-                                  float tmin, float tbest, uint32_t& child_base, uint32_t& tri_base,
-                                  uint32_t& imask) {
+NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravState& s, uint32_t& child_base,
+                                  uint32_t& tri_base, uint32_t& imask) {
     const float4* np = reinterpret_cast<const float4*>(nodes + idx);
     const float4 n0 = __ldg(np + 0);
     const float4 n1 = __ldg(np + 1);
@@ -106,12 +140,13 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, float ox, f
     imask = e >> 24;
     child_base = __float_as_uint(n1.x);
     tri_base = __float_as_uint(n1.y);
-    const float sx = __uint_as_float((e & 0xFFu) << 23) * idx_;
-    const float sy = __uint_as_float(((e >> 8) & 0xFFu) << 23) * idy;
-    const float sz = __uint_as_float(((e >> 16) & 0xFFu) << 23) * idz;
-    const float ax = (n0.x - ox) * idx_;
-    const float ay = (n0.y - oy) * idy;
-    const float az = (n0.z - oz) * idz;
+    const float sx = __uint_as_float((e & 0xFFu) << 23) * s.idx;
+    const float sy = __uint_as_float(((e >> 8) & 0xFFu) << 23) * s.idy;
+    const float sz = __uint_as_float(((e >> 16) & 0xFFu) << 23) * s.idz;
+    const float ax = (n0.x - s.rp.ox) * s.idx;
+    const float ay = (n0.y - s.rp.oy) * s.idy;
+    const float az = (n0.z - s.rp.oz) * s.idz;
+    const bool nx = s.dneg & 1u, ny = s.dneg & 2u, nz = s.dneg & 4u;
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
@@ -122,18 +157,22 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, float ox, f
         const uint32_t qhx = __float_as_uint(half == 0 ? n3.z : n3.w);
         const uint32_t qhy = __float_as_uint(half == 0 ? n4.x : n4.y);
         const uint32_t qhz = __float_as_uint(half == 0 ? n4.z : n4.w);
+        // near / far planes by direction sign: no per-child min/max needed
+        const uint32_t nearx = nx ? qhx : qlx, farx = nx ? qlx : qhx;
+        const uint32_t neary = ny ? qhy : qly, fary = ny ? qly : qhy;
+        const uint32_t nearz = nz ? qhz : qlz, farz = nz ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
-            const float x0 = fmaf(byte_to_float(qlx, j), sx, ax), x1 = fmaf(byte_to_float(qhx, j), sx, ax);
-            const float y0 = fmaf(byte_to_float(qly, j), sy, ay), y1 = fmaf(byte_to_float(qhy, j), sy, ay);
-            const float z0 = fmaf(byte_to_float(qlz, j), sz, az), z1 = fmaf(byte_to_float(qhz, j), sz, az);
-            const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
-            const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tbest));
+            const float x0 = fmaf(byte_to_float(nearx, j), sx, ax), x1 = fmaf(byte_to_float(farx, j), sx, ax);
+            const float y0 = fmaf(byte_to_float(neary, j), sy, ay), y1 = fmaf(byte_to_float(fary, j), sy, ay);
+            const float z0 = fmaf(byte_to_float(nearz, j), sz, az), z1 = fmaf(byte_to_float(farz, j), sz, az);
+            const float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
+            const float tf = fminf(fminf(x1, y1), fminf(z1, s.tmax));
             if (m != 0u && tn * kBoxLo <= tf * kBoxHi) {
                 const uint32_t child_bits = m >> 5;
                 const bool inner = (m & 0x18u) == 0x18u;
-                const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ octinv) : (m & 0x1Fu);
+                const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ s.octinv) : (m & 0x1Fu);
                 hitmask |= child_bits << bit_index;
             }
         }
@@ -141,64 +180,74 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, float ox, f
     return hitmask;
 }
 
-// Walks the compressed BVH8. Returns the BVH-order triangle index of the nearest hit in
-// [tmin, tmax) (ANY_HIT: of any hit) or -1. On a hit tmax is lowered to the hit distance.
-// stack_overflow is set (and the walk abandoned) if the tree is deeper than the stack.
+// One traversal step: visit the highest-priority internal child of the current node group
+// and test the triangles of that node's leaves. Returns true when the ray is finished
+// (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is set, and the ray
+// abandoned, if the tree is deeper than the stack.
+template <bool ANY_HIT, bool STATS>
+NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
+                     bool& stack_overflow, TraceStats* stats) {
+    const uint32_t hits = s.ngroup.y;
+    const int bit = 31 - __clz(hits);
+    s.ngroup.y &= ~(1u << bit);
+    if (s.ngroup.y > 0x00FFFFFFu) {
+        if (s.sp == kTraversalStack) {
+            stack_overflow = true;
+            s.hit = -1;
+            return true;
+        }
+        stack[s.sp++] = s.ngroup;
+    }
+    const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
+    const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+    const uint32_t node = s.ngroup.x + rel;
+    uint32_t child_base, tri_base, imask;
+    const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
+    if (STATS) stats->nodes++;
+    s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
+    uint32_t tmask = hm & 0x00FFFFFFu;
+    while (tmask != 0u) {
+        const int tb = 31 - __clz(tmask);
+        tmask &= ~(1u << tb);
+        const uint32_t ti = tri_base + (uint32_t)tb;
+        const float4* tp = tris + 3 * (size_t)ti;
+        const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+        if (STATS) stats->tris++;
+        float t, u, v;
+        if (tri_intersect(s.rp, p0, p1, p2, s.tmin, s.tmax, t, u, v)) {
+            s.tmax = t;
+            s.hu = u;
+            s.hv = v;
+            s.hit = (int)ti;
+            if (ANY_HIT) return true;
+        }
+    }
+    if (s.ngroup.y <= 0x00FFFFFFu) {
+        if (s.sp == 0) return true;
+        s.ngroup = stack[--s.sp];
+    }
+    return false;
+}
+
+// Whole traversal of one ray (parity hooks and simple callers). Returns the leaf-order
+// triangle index of the nearest hit in [tmin, tmax) (ANY_HIT: of any hit) or -1; on a hit
+// tmax is lowered to the hit distance.
 template <bool ANY_HIT, bool STATS>
 NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__ tris, int num_nodes,
                     float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float& tmax,
                     float& hu, float& hv, bool& stack_overflow, TraceStats* stats) {
     if (num_nodes == 0) return -1;
-    const RayPre rp = ray_precompute(ox, oy, oz, dx, dy, dz);
-    // Clamp tiny direction components so the slab distances stay finite (no 0 * inf).
-    const float kTiny = 1e-20f;
-    const float idx_ = __frcp_rn(fabsf(dx) > kTiny ? dx : copysignf(kTiny, dx));
-    const float idy = __frcp_rn(fabsf(dy) > kTiny ? dy : copysignf(kTiny, dy));
-    const float idz = __frcp_rn(fabsf(dz) > kTiny ? dz : copysignf(kTiny, dz));
-    const uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
-    const uint32_t octinv = 7u - oct;
-
+    TravState s;
+    trav_init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
     uint2 stack[kTraversalStack];
-    int sp = 0;
-    uint2 ngroup = make_uint2(0u, 0x80000000u);  // the root as the only internal hit, imask 0
-    int hit = -1;
-    while (true) {
-        // Visit the highest-priority internal child of the current group.
-        const uint32_t hits = ngroup.y;
-        const int bit = 31 - __clz(hits);
-        ngroup.y &= ~(1u << bit);
-        if (ngroup.y > 0x00FFFFFFu) {
-            if (sp == kTraversalStack) { stack_overflow = true; break; }
-            stack[sp++] = ngroup;
-        }
-        const uint32_t slot = (uint32_t)(bit - 24) ^ octinv;
-        const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
-        const uint32_t node = ngroup.x + rel;
-        uint32_t child_base, tri_base, imask;
-        const uint32_t hm = intersect_children(nodes, node, ox, oy, oz, idx_, idy, idz, octinv, tmin, tmax,
-                                               child_base, tri_base, imask);
-        if (STATS) stats->nodes++;
-        ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-        uint32_t tmask = hm & 0x00FFFFFFu;
-        while (tmask != 0u) {
-            const int tb = 31 - __clz(tmask);
-            tmask &= ~(1u << tb);
-            const uint32_t ti = tri_base + (uint32_t)tb;
-            const float4* tp = tris + 3 * (size_t)ti;
-            const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-            if (STATS) stats->tris++;
-            float t, u, v;
-            if (tri_intersect(rp, p0, p1, p2, tmin, tmax, t, u, v)) {
-                tmax = t; hu = u; hv = v; hit = (int)ti;
-                if (ANY_HIT) return hit;
-            }
-        }
-        if (ngroup.y <= 0x00FFFFFFu) {
-            if (sp == 0) break;
-            ngroup = stack[--sp];
-        }
+    while (!trav_step<ANY_HIT, STATS>(s, stack, nodes, tris, stack_overflow, stats)) {
     }
-    return hit;
+    if (s.hit >= 0) {
+        tmax = s.tmax;
+        hu = s.hu;
+        hv = s.hv;
+    }
+    return s.hit;
 }
 
 }  // namespace ngi

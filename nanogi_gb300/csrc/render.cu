@@ -7,9 +7,10 @@
 //              next direction; a finished slot immediately claims the next sample index
 //              (path regeneration) and starts a camera path. Extension and shadow rays are
 //              appended to compacted queues with one atomic per warp.
-//   k_extend : closest-hit traversal of the extension queue (compressed BVH8)
-//   k_shadow : any-hit traversal of the shadow queue; unoccluded contributions are added
-//              to the FP64 film with atomics.
+//   k_trace<extension> : closest-hit traversal of the extension queue (compressed BVH8)
+//   k_trace<shadow>    : any-hit traversal of the shadow queue; unoccluded contributions
+//                        are added to the FP64 film with atomics.
+// Both traversal kernels are persistent: resident warps refill idle lanes from the queue.
 // Iterations are captured in a CUDA graph and replayed until every slot has drained.
 #include <cuda_runtime.h>
 
@@ -43,6 +44,8 @@ struct WaveCounters {
     int ext_count;
     int sh_count;
     int active;
+    int ext_fetch;                    // rays handed out by the persistent extension kernel
+    int sh_fetch;                     // rays handed out by the persistent shadow kernel
     int error_flags;                  // bit 0: traversal stack overflow
     unsigned long long stat_camera;
     unsigned long long stat_ext;
@@ -61,6 +64,7 @@ struct RenderConsts {
     int width, height;
     int stratified;
     long long strat_end;    // global sample indices below this are pixel-stratified
+    int trace_refill;       // idle lanes that trigger a traversal warp's refill
 };
 
 template <typename R>
@@ -430,54 +434,79 @@ NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
     if (lane_id() == 0 && x) atomicAdd(counter, x);
 }
 
-template <typename R, bool STATS>
-__global__ void __launch_bounds__(256) k_extend(SceneView<R> sv, WaveView<R> w) {
-    const int n = w.ctr->ext_count;
+// ---- persistent traversal -------------------------------------------------------------------
+// Warps stay resident and trace until both the queue and their lanes are empty. A lane
+// whose ray has finished sits idle until at least `refill` lanes of its warp are idle; then
+// the warp fetches that many new rays with one atomic and the lanes start them while the
+// others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
+// and removes the tail of a fixed grid.
+template <typename R, bool SHADOW, bool STATS>
+__global__ void __launch_bounds__(128) k_trace(SceneView<R> sv, WaveView<R> w, int refill) {
+    const int n = SHADOW ? w.ctr->sh_count : w.ctr->ext_count;
+    int* fetch = SHADOW ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
+    TravState s;
+    uint2 stack[kTraversalStack];
+    int item = -1, slot = -1;
+    bool exhausted = false;
     bool overflow = false;
     TraceStats ts{0u, 0u};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int s = w.ext_queue[i];
-        const float4 o = w.ray_o[s], d = w.ray_d[s];
-        float tmax = d.w, u = 0.0f, v = 0.0f;
-        const int ti = trace_ray<false, STATS>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
-                                               tmax, u, v, overflow, &ts);
-        w.hit[s] = make_float4(tmax, u, v, __int_as_float(ti));
-    }
-    if (overflow) atomicOr(&w.ctr->error_flags, 1);
-    if (STATS) {
-        warp_sum_add(&w.ctr->ext_nodes, ts.nodes);
-        warp_sum_add(&w.ctr->ext_tris, ts.tris);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_ext, (unsigned long long)n);
-}
-
-template <typename R, bool STATS>
-__global__ void __launch_bounds__(256) k_shadow(SceneView<R> sv, WaveView<R> w) {
-    const int n = w.ctr->sh_count;
-    bool overflow = false;
-    TraceStats ts{0u, 0u};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = w.sh_o[i], d = w.sh_d[i];
-        float tmax = d.w, u, v;
-        const int ti = trace_ray<true, STATS>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
-                                              tmax, u, v, overflow, &ts);
-        if (ti < 0) {
-            const Vec4T<R> c = w.sh_c[i];
-            const V3<R> cc = v3<R>(c.x, c.y, c.z);
-            if (finite3(cc)) {
-                film_add(w.film, w.sh_pix[i], cc);
-                atomicAdd(&w.ctr->stat_contrib, 1ull);
-            } else {
-                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+    while (true) {
+        const bool idle = item < 0;
+        const unsigned idle_mask = __ballot_sync(0xFFFFFFFFu, idle);
+        if (!exhausted && __popc(idle_mask) >= refill) {
+            const int leader = __ffs(idle_mask) - 1;
+            int base = 0;
+            if ((int)lane_id() == leader) base = atomicAdd(fetch, __popc(idle_mask));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (base + __popc(idle_mask) >= n) exhausted = true;
+            if (idle) {
+                const int i = base + __popc(idle_mask & lanemask_lt());
+                if (i < n) {
+                    item = i;
+                    float4 o, d;
+                    if (SHADOW) {
+                        o = w.sh_o[i];
+                        d = w.sh_d[i];
+                    } else {
+                        slot = w.ext_queue[i];
+                        o = w.ray_o[slot];
+                        d = w.ray_d[slot];
+                    }
+                    trav_init(s, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
+                }
+            }
+        }
+        const unsigned busy = __ballot_sync(0xFFFFFFFFu, item >= 0);
+        if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
+        if (item >= 0) {
+            const bool done = sv.num_nodes == 0 ||
+                              trav_step<SHADOW, STATS>(s, stack, sv.nodes, sv.tris, overflow, &ts);
+            if (done) {
+                if (SHADOW) {
+                    if (s.hit < 0) {
+                        const Vec4T<R> c = w.sh_c[item];
+                        const V3<R> cc = v3<R>(c.x, c.y, c.z);
+                        if (finite3(cc)) {
+                            film_add(w.film, w.sh_pix[item], cc);
+                            atomicAdd(&w.ctr->stat_contrib, 1ull);
+                        } else {
+                            atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                        }
+                    }
+                } else {
+                    w.hit[slot] = make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit));
+                }
+                item = -1;
             }
         }
     }
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
     if (STATS) {
-        warp_sum_add(&w.ctr->sh_nodes, ts.nodes);
-        warp_sum_add(&w.ctr->sh_tris, ts.tris);
+        warp_sum_add(SHADOW ? &w.ctr->sh_nodes : &w.ctr->ext_nodes, ts.nodes);
+        warp_sum_add(SHADOW ? &w.ctr->sh_tris : &w.ctr->ext_tris, ts.tris);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&w.ctr->stat_shadow, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(SHADOW ? &w.ctr->stat_shadow : &w.ctr->stat_ext, (unsigned long long)n);
 }
 
 // ---- parity hooks --------------------------------------------------------------------------
@@ -762,18 +791,48 @@ int grid_for(int items, int block) {
     return std::max(1, std::min(max_blocks, (items + block - 1) / block));
 }
 
+// Blocks of a persistent kernel that fit on the device at once.
+template <typename K>
+int persistent_grid(K kernel, int block) {
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    return std::max(1, sms * std::max(per_sm, 1));
+}
+
+constexpr int kTraceBlock = 128;
+constexpr int kRefillLanes = 8;
+
+// Grid sizes of the persistent traversal kernels (queried once, outside any graph capture).
+template <typename R, bool STATS>
+struct TraceGrids {
+    static int ext() {
+        static const int g = persistent_grid(k_trace<R, false, STATS>, kTraceBlock);
+        return g;
+    }
+    static int shadow() {
+        static const int g = persistent_grid(k_trace<R, true, STATS>, kTraceBlock);
+        return g;
+    }
+};
+
 template <typename R, bool DIRECT, bool STATS>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
                        int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev) {
+    (void)g_trace;
+    const int g_ext = TraceGrids<R, STATS>::ext();
+    const int g_sh = TraceGrids<R, STATS>::shadow();
     const size_t off = offsetof(WaveCounters, ext_count);
     const size_t len = offsetof(WaveCounters, error_flags) - off;
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
     k_logic<R, DIRECT><<<g_logic, 256, 0, stream>>>(sv, v, rc);
     if (ev) cudaEventRecord(ev[1], stream);
-    k_extend<R, STATS><<<g_trace, 256, 0, stream>>>(sv, v);
+    const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
+    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_shadow<R, STATS><<<g_trace, 256, 0, stream>>>(sv, v);
+    k_trace<R, true, STATS><<<g_sh, kTraceBlock, 0, stream>>>(sv, v, refill);
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
@@ -788,6 +847,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
 
+    TraceGrids<R, STATS>::ext();
+    TraceGrids<R, STATS>::shadow();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
@@ -899,6 +960,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    rc.trace_refill = p.trace_refill;
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
@@ -1157,6 +1219,7 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
     rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    rc.trace_refill = p.trace_refill;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
     if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v{};
