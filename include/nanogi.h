@@ -83,6 +83,8 @@ typedef struct ngi_render_params {
     int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
     int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
     int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
+    int32_t trace_postpone;    /* triangle tests wait while fewer than (value-1)% of a warp's lanes have
+                                  some (1..101, 1 = never wait); 0 = auto */
 } ngi_render_params;
 
 /* Measurement flags (results in ngi_render_stats). Both change only how the render is
@@ -191,6 +193,23 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
  *     the GPU (e.g. from two streams at once) race on it and must not be made. */
 NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_params* params,
                                              double* d_film_rgb, void* stream);
+
+/* ---- differentiable rendering (no counterpart in the reference) ---------------------- */
+
+/* Reads / replaces the differentiable parameters of every primitive: `albedo` is the R of
+ * the BSDF used at hits (D.R, else G.R, else S.*.R; rt.hpp:439-476), `emission` the Le of a
+ * light (rt.hpp:395-415). Arrays hold num_primitives*3 doubles; either may be NULL. Entries of
+ * primitives without a BSDF / without L are ignored on write and zero on read. Updates the
+ * device tables in place when the scene is built (no reload, no BVH rebuild). */
+NGI_API ngi_status ngi_scene_get_parameters(const ngi_scene* scene, double* albedo, double* emission);
+NGI_API ngi_status ngi_scene_set_parameters(ngi_scene* scene, const double* albedo, const double* emission);
+
+/* Path-replay adjoint of ngi_render with the same params (seed included): replays the same
+ * paths, recomputing rather than storing them, and returns dLoss/dalbedo and dLoss/demission
+ * (num_primitives*3 doubles each, overwritten) for d_film = dLoss/d(film), the HOST gradient
+ * of the normalised film ngi_render returned. Requires max_num_vertices in 1..17. */
+NGI_API ngi_status ngi_render_backward(ngi_scene* scene, const ngi_render_params* params, const double* d_film,
+                                       double* grad_albedo, double* grad_emission);
 
 /* ---- parity hooks ------------------------------------------------------------------ */
 

@@ -102,6 +102,21 @@ class Scene:
         check(load_library().ngi_visible(self.handle, _ptr(pairs), pairs.shape[0], _ptr(out)))
         return out.astype(bool)
 
+    def parameters(self):
+        """(albedo, emission): (num_primitives, 3) float64 arrays of R and Le."""
+        n = self.info()["num_primitives"]
+        a = np.empty((n, 3), np.float64)
+        e = np.empty((n, 3), np.float64)
+        check(load_library().ngi_scene_get_parameters(self.handle, _ptr(a), _ptr(e)))
+        return a, e
+
+    def set_parameters(self, albedo=None, emission=None) -> None:
+        n = self.info()["num_primitives"]
+        a = None if albedo is None else np.ascontiguousarray(albedo, np.float64).reshape(n, 3)
+        e = None if emission is None else np.ascontiguousarray(emission, np.float64).reshape(n, 3)
+        check(load_library().ngi_scene_set_parameters(self.handle, None if a is None else _ptr(a),
+                                                      None if e is None else _ptr(e)))
+
     def last_stats(self) -> dict:
         st = RenderStats()
         check(load_library().ngi_get_render_stats(self.handle, ctypes.byref(st)))
@@ -125,6 +140,7 @@ class Renderer:
     iterations_per_graph: int = 0
     flags: int = 0
     trace_refill: int = 0
+    trace_postpone: int = 0
     last_stats: dict = field(default_factory=dict, repr=False)
 
     def params(self) -> RenderParams:
@@ -144,6 +160,7 @@ class Renderer:
             iterations_per_graph=int(self.iterations_per_graph),
             flags=int(self.flags),
             trace_refill=int(self.trace_refill),
+            trace_postpone=int(self.trace_postpone),
         )
 
     def render(self, scene: Scene, film: np.ndarray | None = None) -> np.ndarray:
@@ -156,6 +173,19 @@ class Renderer:
         check(load_library().ngi_render(scene.handle, ctypes.byref(p), _ptr(film)))
         self.last_stats = scene.last_stats()
         return film
+
+    def backward(self, scene: Scene, d_film: np.ndarray):
+        """Path-replay adjoint of render(): dLoss/dalbedo, dLoss/demission per primitive."""
+        p = self.params()
+        d = np.ascontiguousarray(d_film, np.float64)
+        if d.size != 3 * self.width * self.height:
+            raise ValueError("d_film must hold width*height*3 values")
+        n = scene.info()["num_primitives"]
+        ga = np.empty((n, 3), np.float64)
+        ge = np.empty((n, 3), np.float64)
+        check(load_library().ngi_render_backward(scene.handle, ctypes.byref(p), _ptr(d), _ptr(ga), _ptr(ge)))
+        self.last_stats = scene.last_stats()
+        return ga, ge
 
     def render_device(self, scene: Scene, d_film_ptr: int, stream: int = 0) -> None:
         """Adds raw (un-normalised) sums into a device film (e.g. a torch.cuda tensor's data_ptr)."""

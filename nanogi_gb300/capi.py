@@ -43,6 +43,7 @@ class RenderParams(ctypes.Structure):
         ("iterations_per_graph", ctypes.c_int32),
         ("flags", ctypes.c_int32),
         ("trace_refill", ctypes.c_int32),
+        ("trace_postpone", ctypes.c_int32),
     ]
 
 
@@ -105,6 +106,10 @@ PROTOTYPES = {
     "ngi_get_render_stats": (ctypes.c_int, [ctypes.c_void_p, _P(RenderStats)]),
     "ngi_render_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p,
                                                  ctypes.c_void_p]),
+    "ngi_scene_get_parameters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ngi_scene_set_parameters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ngi_render_backward": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
     "ngi_intersect": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_visible": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),

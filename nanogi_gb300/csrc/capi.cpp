@@ -1,5 +1,6 @@
 // C ABI of nanogi-gb300 (include/nanogi.h): status codes, thread-local error text, no
 // exception ever crosses the boundary.
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -69,6 +70,8 @@ ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
         return Fail(NGI_ERR_INVALID_ARGUMENT, "wave_size / iterations_per_graph out of range");
     if (p->trace_refill < 0 || p->trace_refill > 32)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_refill must be 0 (auto) or 1..32");
+    if (p->trace_postpone < 0 || p->trace_postpone > 101)
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_postpone must be 0 (auto) or 1..101");
     return NGI_OK;
 }
 
@@ -186,6 +189,55 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
     }
     g_last_error.clear();
     return NGI_OK;
+}
+
+NGI_API ngi_status ngi_scene_get_parameters(const ngi_scene* scene, double* albedo, double* emission) {
+    if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
+    const ngi::HostScene& h = *scene->host;
+    for (size_t i = 0; i < h.prims.size(); i++) {
+        const ngi::HostPrimitive& p = h.prims[i];
+        const double* r = (p.type & ngi::PT_D) ? p.D_R : (p.type & ngi::PT_G) ? p.G_R : (p.type & ngi::PT_S) ? p.S_R : nullptr;
+        for (int k = 0; k < 3; k++) {
+            if (albedo) albedo[3 * i + k] = r ? r[k] : 0.0;
+            if (emission) emission[3 * i + k] = (p.type & ngi::PT_L) ? p.Le[k] : 0.0;
+        }
+    }
+    g_last_error.clear();
+    return NGI_OK;
+}
+
+NGI_API ngi_status ngi_scene_set_parameters(ngi_scene* scene, const double* albedo, const double* emission) {
+    if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
+    return Guard([&]() {
+        ngi::HostScene& h = *scene->host;
+        for (size_t i = 0; i < h.prims.size(); i++) {
+            ngi::HostPrimitive& p = h.prims[i];
+            double* r = (p.type & ngi::PT_D) ? p.D_R : (p.type & ngi::PT_G) ? p.G_R : (p.type & ngi::PT_S) ? p.S_R : nullptr;
+            for (int k = 0; k < 3; k++) {
+                if (albedo && r) {
+                    if (!std::isfinite(albedo[3 * i + k])) return Fail(NGI_ERR_INVALID_ARGUMENT, "albedo must be finite");
+                    r[k] = albedo[3 * i + k];
+                }
+                if (emission && (p.type & ngi::PT_L)) {
+                    if (!std::isfinite(emission[3 * i + k])) return Fail(NGI_ERR_INVALID_ARGUMENT, "emission must be finite");
+                    p.Le[k] = emission[3 * i + k];
+                }
+            }
+        }
+        ngi::DeviceUpdateTables(h);
+        return NGI_OK;
+    });
+}
+
+NGI_API ngi_status ngi_render_backward(ngi_scene* scene, const ngi_render_params* params, const double* d_film,
+                                       double* grad_albedo, double* grad_emission) {
+    const ngi_status st = CheckParams(scene, params);
+    if (st != NGI_OK) return st;
+    if (!d_film) return Fail(NGI_ERR_INVALID_ARGUMENT, "d_film is NULL");
+    return Guard([&]() {
+        ngi::DeviceRenderBackward(*scene->host, *params, d_film, grad_albedo, grad_emission);
+        return NGI_OK;
+    });
 }
 
 NGI_API ngi_status ngi_intersect(ngi_scene* scene, const float* rays, int64_t n, int32_t* prim_out, float* t_out,

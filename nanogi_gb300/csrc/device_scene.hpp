@@ -54,6 +54,11 @@ struct DeviceScene {
     // film used by the host-buffer render entry point (kept between calls)
     double* film = nullptr;
     size_t film_elems = 0;
+    // adjoint: dLoss/dfilm and the gradient accumulators (kept between calls)
+    double* adj = nullptr;
+    size_t adj_elems = 0;
+    double* grads = nullptr;
+    size_t grad_elems = 0;
 };
 
 // Uploads the flattened scene and builds the BVH on the current device.
@@ -72,6 +77,14 @@ void DeviceRenderToHost(HostScene& scene, const ngi_render_params& params, doubl
 // Same render with all scratch in a fixed file-scope device array: allocates nothing.
 // Needs the scene built beforehand; bounds the wave at 65536 path slots.
 void DeviceRenderNoAlloc(HostScene& scene, const ngi_render_params& params, double* d_film, cudaStream_t stream);
+
+// Path-replay adjoint of DeviceRenderToHost: replays the same paths and accumulates
+// dLoss/dR (BSDF albedo) and dLoss/dLe per primitive from h_dfilm = dLoss/d(normalised film).
+void DeviceRenderBackward(HostScene& scene, const ngi_render_params& params, const double* h_dfilm,
+                          double* grad_albedo, double* grad_emission);
+
+// Pushes the host copy of the materials / lights (after a parameter update) to the device.
+void DeviceUpdateTables(HostScene& scene);
 
 // Parity hooks.
 void DeviceIntersect(HostScene& scene, const float* h_rays, int64_t n, int32_t* prim, float* t, float* uv);

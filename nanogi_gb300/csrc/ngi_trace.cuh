@@ -180,36 +180,55 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
     return hitmask;
 }
 
-// One traversal step: visit the highest-priority internal child of the current node group
-// and test the triangles of that node's leaves. Returns true when the ray is finished
-// (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is set, and the ray
-// abandoned, if the tree is deeper than the stack.
+// One traversal step (Ylitie, Karras, Laine 2017, with triangle postponing). A step either
+// visits the highest-priority internal child of the current node group, or takes up a
+// triangle group popped from the stack. Triangle tests are postponed (the group pushed on
+// the stack) while fewer than `postpone_pct` percent of the warp's active lanes have
+// triangles to test, so that tests run together instead of one lane at a time. Returns true
+// when the ray is finished (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is
+// set, and the ray abandoned, if the tree is deeper than the stack.
 template <bool ANY_HIT, bool STATS>
 NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
-                     bool& stack_overflow, TraceStats* stats) {
-    const uint32_t hits = s.ngroup.y;
-    const int bit = 31 - __clz(hits);
-    s.ngroup.y &= ~(1u << bit);
+                     bool& stack_overflow, TraceStats* stats, int postpone_pct) {
+    uint2 tgroup;
     if (s.ngroup.y > 0x00FFFFFFu) {
-        if (s.sp == kTraversalStack) {
-            stack_overflow = true;
-            s.hit = -1;
-            return true;
+        const uint32_t hits = s.ngroup.y;
+        const int bit = 31 - __clz(hits);
+        s.ngroup.y &= ~(1u << bit);
+        if (s.ngroup.y > 0x00FFFFFFu) {
+            if (s.sp == kTraversalStack) {
+                stack_overflow = true;
+                s.hit = -1;
+                return true;
+            }
+            stack[s.sp++] = s.ngroup;
         }
-        stack[s.sp++] = s.ngroup;
+        const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
+        const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+        const uint32_t node = s.ngroup.x + rel;
+        uint32_t child_base, tri_base, imask;
+        const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
+        if (STATS) stats->nodes++;
+        s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
+        tgroup = make_uint2(tri_base, hm & 0x00FFFFFFu);
+    } else {
+        tgroup = s.ngroup;  // a postponed triangle group taken off the stack
+        s.ngroup = make_uint2(0u, 0u);
     }
-    const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
-    const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
-    const uint32_t node = s.ngroup.x + rel;
-    uint32_t child_base, tri_base, imask;
-    const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
-    if (STATS) stats->nodes++;
-    s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-    uint32_t tmask = hm & 0x00FFFFFFu;
-    while (tmask != 0u) {
-        const int tb = 31 - __clz(tmask);
-        tmask &= ~(1u << tb);
-        const uint32_t ti = tri_base + (uint32_t)tb;
+    if (postpone_pct > 0) {
+        const unsigned act = __activemask();
+        const bool has_tri = tgroup.y != 0u;
+        const unsigned tri_lanes = __ballot_sync(act, has_tri);
+        const bool more = s.ngroup.y > 0x00FFFFFFu || s.sp > 0;
+        if (has_tri && more && s.sp < kTraversalStack - 1 && __popc(tri_lanes) * 100 < __popc(act) * postpone_pct) {
+            stack[s.sp++] = tgroup;
+            tgroup.y = 0u;
+        }
+    }
+    while (tgroup.y != 0u) {
+        const int tb = 31 - __clz(tgroup.y);
+        tgroup.y &= ~(1u << tb);
+        const uint32_t ti = tgroup.x + (uint32_t)tb;
         const float4* tp = tris + 3 * (size_t)ti;
         const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
         if (STATS) stats->tris++;
@@ -229,6 +248,8 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
     return false;
 }
 
+constexpr int kPostponePct = 20;
+
 // Whole traversal of one ray (parity hooks and simple callers). Returns the leaf-order
 // triangle index of the nearest hit in [tmin, tmax) (ANY_HIT: of any hit) or -1; on a hit
 // tmax is lowered to the hit distance.
@@ -240,7 +261,7 @@ NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__
     TravState s;
     trav_init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
     uint2 stack[kTraversalStack];
-    while (!trav_step<ANY_HIT, STATS>(s, stack, nodes, tris, stack_overflow, stats)) {
+    while (!trav_step<ANY_HIT, STATS>(s, stack, nodes, tris, stack_overflow, stats, 0)) {
     }
     if (s.hit >= 0) {
         tmax = s.tmax;

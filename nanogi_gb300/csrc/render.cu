@@ -37,6 +37,11 @@ namespace ngi {
 
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 
+// Minimum resident blocks per SM asked of the traversal kernels (register budget).
+#ifndef NGI_TRACE_MIN_BLOCKS
+#define NGI_TRACE_MIN_BLOCKS 8
+#endif
+
 enum : uint8_t { SLOT_EMPTY = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
 
 struct WaveCounters {
@@ -65,6 +70,7 @@ struct RenderConsts {
     int stratified;
     long long strat_end;    // global sample indices below this are pixel-stratified
     int trace_refill;       // idle lanes that trigger a traversal warp's refill
+    int trace_postpone;     // triangle-postponing threshold (percent of active lanes), -1 = default
 };
 
 template <typename R>
@@ -87,11 +93,22 @@ struct WaveView {
     uint32_t* sh_pix;
     WaveCounters* ctr;
     double* film;
+    // path-replay adjoint only (null otherwise)
+    uint4* pre;              // per slot: 2 x uint4 = up to 16 primitive ids (uint16) of the path's surface vertices
+    uint4* sh_pre;           // per shadow ray: the same prefix
+    int2* sh_info;           // per shadow ray: x = prefix length | (NEE-vertex primitive + 1) << 8, y = light primitive
+    const double* adj;       // dLoss/dfilm per pixel and channel, scaled by W*H/N
+    double* grad_albedo;     // per primitive x 3
+    double* grad_emission;   // per primitive x 3
 };
+
+// Longest surface-vertex prefix the adjoint carries: paths of up to 17 vertices.
+constexpr int kAdjMaxPrefix = 16;
 
 struct RenderWave {
     int Q = 0;
     int precision = -1;
+    bool adjoint_buffers = false;
     std::vector<void*> bufs;
     WaveCounters* ctr = nullptr;
     WaveCounters* h_ctr = nullptr;   // pinned
@@ -138,7 +155,50 @@ struct ShadowRay {
     float ox, oy, oz, dx, dy, dz, tmax;
     V3<R> c;
     uint32_t pixel;
+    int light_prim;  // adjoint: primitive whose Le scales the contribution
 };
+
+// Primitive id k of a path prefix held in two uint4 (16 x uint16).
+NGI_D uint32_t prefix_get(const uint4& a, const uint4& b, int k) {
+    const uint4& q = k < 8 ? a : b;
+    const int j = (k & 7) >> 1;
+    const uint32_t word = j == 0 ? q.x : (j == 1 ? q.y : (j == 2 ? q.z : q.w));
+    return (k & 1) ? (word >> 16) : (word & 0xFFFFu);
+}
+NGI_D void prefix_set(uint4& a, uint4& b, int k, uint32_t prim) {
+    uint4& q = k < 8 ? a : b;
+    const int j = (k & 7) >> 1;
+    uint32_t& word = j == 0 ? q.x : (j == 1 ? q.y : (j == 2 ? q.z : q.w));
+    word = (k & 1) ? ((word & 0x0000FFFFu) | (prim << 16)) : ((word & 0xFFFF0000u) | (prim & 0xFFFFu));
+}
+
+// Path-replay gradient of one film contribution C at `pixel` (Vicini, Speierer, Jakob 2021):
+// every sampling decision of pt/ptdirect is independent of the albedo R and the emission Le,
+// and C is a product holding R of each surface vertex on its path (the prefix, plus the
+// NEE vertex) and one Le, so dC/dR_m = C * n_m / R_m and dC/dLe = C / Le, channel by channel.
+template <typename R>
+NGI_D void adj_accumulate(const WaveView<R>& w, const SceneView<R>& sv, uint32_t pixel, V3<R> C, const uint4& pa,
+                          const uint4& pb, int count, int vertex_prim, int light_prim) {
+    const double* a = w.adj + 3 * (size_t)pixel;
+    const double wc[3] = {a[0] * (double)C.x, a[1] * (double)C.y, a[2] * (double)C.z};
+    if (wc[0] == 0.0 && wc[1] == 0.0 && wc[2] == 0.0) return;
+    auto add_albedo = [&](int m) {
+        const V3<R> r = sv.mats[m].R_;
+        const double rc[3] = {(double)r.x, (double)r.y, (double)r.z};
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (rc[c] != 0.0) atomicAdd(w.grad_albedo + 3 * (size_t)m + c, wc[c] / rc[c]);
+    };
+    for (int k = 0; k < count; k++) add_albedo((int)prefix_get(pa, pb, k));
+    if (vertex_prim >= 0) add_albedo(vertex_prim);
+    if (light_prim >= 0) {
+        const V3<R> le = sv.mats[light_prim].Le;
+        const double lc[3] = {(double)le.x, (double)le.y, (double)le.z};
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            if (lc[c] != 0.0) atomicAdd(w.grad_emission + 3 * (size_t)light_prim + c, wc[c] / lc[c]);
+    }
+}
 
 // Next-event estimation at a vertex (src/nanogi.cpp:654-707).
 template <typename R>
@@ -199,6 +259,7 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
     out.tmax = (float)len * (1.0f - kEpsF);
     out.c = C;
     out.pixel = pix;
+    out.light_prim = L.prim;
 }
 
 template <typename R>
@@ -211,7 +272,7 @@ NGI_D void store_ray(const WaveView<R>& w, int s, V3<R> o, V3<R> d) {
     }
 }
 
-template <typename R, bool DIRECT>
+template <typename R, bool DIRECT, bool ADJ>
 __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
@@ -221,6 +282,8 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
         bool want_ext = false;
         ShadowRay<R> sa;
         sa.valid = false;
+        uint4 pa = make_uint4(0u, 0u, 0u, 0u), pb = pa;  // adjoint: surface-vertex prefix of the path
+        int sa_count = 0, sa_vprim = -1;
 
         if (st == SLOT_ACTIVE) {
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
@@ -262,14 +325,23 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 g.uvx = R(0); g.uvy = R(0);
                 const int prim = __float_as_int(m1.w);
                 const DevMaterial<R>& mat = sv.mats[prim];
+                if (ADJ) {
+                    pa = w.pre[2 * (size_t)s];
+                    pb = w.pre[2 * (size_t)s + 1];
+                }
 
                 if (!DIRECT && (mat.type & DT_L) && mat.l_type == LT_AREA) {
                     // Emission on a light hit (src/nanogi.cpp:568-575)
                     if (dot(g.sn, -d) > R(0)) {
                         const V3<R> c = thr * mat.Le;
                         if (!is_zero(c)) {
-                            if (finite3(c)) { film_add(w.film, pixel, c); atomicAdd(&w.ctr->stat_contrib, 1ull); }
-                            else atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                            if (finite3(c)) {
+                                film_add(w.film, pixel, c);
+                                atomicAdd(&w.ctr->stat_contrib, 1ull);
+                                if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim);
+                            } else {
+                                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                            }
                         }
                     }
                 }
@@ -284,6 +356,8 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                         if (DIRECT) {
                             const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
                             next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
+                            sa_count = nv - 2;
+                            sa_vprim = prim;
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
                         V3<R> wo;
@@ -292,6 +366,15 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                             const V3<R> fs = bsdf_eval(mat, g, wi, wo, true);
                             if (!is_zero(fs)) {
                                 thr = thr * fs / pdf;
+                                if (ADJ) {
+                                    if (nv - 2 >= kAdjMaxPrefix) {
+                                        atomicOr(&w.ctr->error_flags, 2);
+                                    } else {
+                                        prefix_set(pa, pb, nv - 2, (uint32_t)prim);
+                                        w.pre[2 * (size_t)s] = pa;
+                                        w.pre[2 * (size_t)s + 1] = pb;
+                                    }
+                                }
                                 store_ray(w, s, g.p, wo);
                                 w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
                                 w.nverts[s] = nv;
@@ -313,6 +396,11 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 w.sh_d[q] = make_float4(sa.dx, sa.dy, sa.dz, sa.tmax);
                 w.sh_c[q] = Vec4T<R>{sa.c.x, sa.c.y, sa.c.z, R(0)};
                 w.sh_pix[q] = sa.pixel;
+                if (ADJ) {
+                    w.sh_pre[2 * (size_t)q] = pa;
+                    w.sh_pre[2 * (size_t)q + 1] = pb;
+                    w.sh_info[q] = make_int2(sa_count | ((sa_vprim + 1) << 8), sa.light_prim);
+                }
             }
         }
 
@@ -332,6 +420,10 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
             if (need_new) {
                 if (k >= (unsigned long long)rc.num_samples) {
                     st = SLOT_DONE;
+                } else if (rc.max_vertices == 1) {
+                    // the loop's first test ends the path before the sensor vertex does anything
+                    // (src/nanogi.cpp:485, 647): the sample counts, nothing is traced
+                    st = SLOT_EMPTY;
                 } else {
                     // ---- sensor vertex (src/nanogi.cpp:450-479, 609-641) ----
                     const unsigned long long gsample = (unsigned long long)rc.sample_offset + k;
@@ -413,6 +505,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 w.sh_d[q] = make_float4(sb.dx, sb.dy, sb.dz, sb.tmax);
                 w.sh_c[q] = Vec4T<R>{sb.c.x, sb.c.y, sb.c.z, R(0)};
                 w.sh_pix[q] = sb.pixel;
+                if (ADJ) w.sh_info[q] = make_int2(0, sb.light_prim);  // sensor vertex: no surface factors
             }
         }
         {
@@ -440,8 +533,8 @@ NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
 // the warp fetches that many new rays with one atomic and the lanes start them while the
 // others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
 // and removes the tail of a fixed grid.
-template <typename R, bool SHADOW, bool STATS>
-__global__ void __launch_bounds__(128) k_trace(SceneView<R> sv, WaveView<R> w, int refill) {
+template <typename R, bool SHADOW, bool STATS, bool ADJ = false>
+__global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone) {
     const int n = SHADOW ? w.ctr->sh_count : w.ctr->ext_count;
     int* fetch = SHADOW ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
     TravState s;
@@ -480,15 +573,26 @@ __global__ void __launch_bounds__(128) k_trace(SceneView<R> sv, WaveView<R> w, i
         if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
         if (item >= 0) {
             const bool done = sv.num_nodes == 0 ||
-                              trav_step<SHADOW, STATS>(s, stack, sv.nodes, sv.tris, overflow, &ts);
+                              trav_step<SHADOW, STATS>(s, stack, sv.nodes, sv.tris, overflow, &ts, postpone);
             if (done) {
                 if (SHADOW) {
                     if (s.hit < 0) {
                         const Vec4T<R> c = w.sh_c[item];
                         const V3<R> cc = v3<R>(c.x, c.y, c.z);
                         if (finite3(cc)) {
-                            film_add(w.film, w.sh_pix[item], cc);
+                            const uint32_t pix = w.sh_pix[item];
+                            film_add(w.film, pix, cc);
                             atomicAdd(&w.ctr->stat_contrib, 1ull);
+                            if (ADJ) {
+                                const int2 info = w.sh_info[item];
+                                const int count = info.x & 0xFF;
+                                uint4 qa = make_uint4(0u, 0u, 0u, 0u), qb = qa;
+                                if (count > 0) {
+                                    qa = w.sh_pre[2 * (size_t)item];
+                                    qb = w.sh_pre[2 * (size_t)item + 1];
+                                }
+                                adj_accumulate(w, sv, pix, cc, qa, qb, count, (info.x >> 8) - 1, info.y);
+                            }
                         } else {
                             atomicAdd(&w.ctr->stat_nonfinite, 1ull);
                         }
@@ -716,7 +820,7 @@ void DeviceFree(HostScene& hs) {
     if (ds->stream) cudaStreamSynchronize(ds->stream);
     free_wave(ds->wave);
     void* ptrs[] = {ds->nodes, ds->tris, ds->nrm, ds->uv, ds->mats_f, ds->mats_d, ds->lights_f,
-                    ds->lights_d, ds->cdf, ds->emit_pos, ds->emit_uv, ds->film};
+                    ds->lights_d, ds->cdf, ds->emit_pos, ds->emit_uv, ds->film, ds->adj, ds->grads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (ds->stream) cudaStreamDestroy(ds->stream);
@@ -805,38 +909,39 @@ constexpr int kTraceBlock = 128;
 constexpr int kRefillLanes = 8;
 
 // Grid sizes of the persistent traversal kernels (queried once, outside any graph capture).
-template <typename R, bool STATS>
+template <typename R, bool STATS, bool ADJ = false>
 struct TraceGrids {
     static int ext() {
         static const int g = persistent_grid(k_trace<R, false, STATS>, kTraceBlock);
         return g;
     }
     static int shadow() {
-        static const int g = persistent_grid(k_trace<R, true, STATS>, kTraceBlock);
+        static const int g = persistent_grid(k_trace<R, true, STATS, ADJ>, kTraceBlock);
         return g;
     }
 };
 
-template <typename R, bool DIRECT, bool STATS>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
                        int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev) {
     (void)g_trace;
-    const int g_ext = TraceGrids<R, STATS>::ext();
-    const int g_sh = TraceGrids<R, STATS>::shadow();
+    const int g_ext = TraceGrids<R, STATS, ADJ>::ext();
+    const int g_sh = TraceGrids<R, STATS, ADJ>::shadow();
     const size_t off = offsetof(WaveCounters, ext_count);
     const size_t len = offsetof(WaveCounters, error_flags) - off;
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
-    k_logic<R, DIRECT><<<g_logic, 256, 0, stream>>>(sv, v, rc);
+    k_logic<R, DIRECT, ADJ><<<g_logic, 256, 0, stream>>>(sv, v, rc);
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
-    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill);
+    const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
+    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_trace<R, true, STATS><<<g_sh, kTraceBlock, 0, stream>>>(sv, v, refill);
+    k_trace<R, true, STATS, ADJ><<<g_sh, kTraceBlock, 0, stream>>>(sv, v, refill, postpone);
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
-template <typename R, bool DIRECT, bool STATS>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
               bool kernel_timing, cudaStream_t stream) {
     DeviceScene& ds = *hs.dev;
@@ -847,14 +952,14 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
 
-    TraceGrids<R, STATS>::ext();
-    TraceGrids<R, STATS>::shadow();
+    TraceGrids<R, STATS, ADJ>::ext();
+    TraceGrids<R, STATS, ADJ>::shadow();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < iters_per_graph; it++)
-            enqueue_iteration<R, DIRECT, STATS>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr);
+            enqueue_iteration<R, DIRECT, STATS, ADJ>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr);
         const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
         if (cap != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
@@ -879,7 +984,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
         while (true) {
             if (kernel_timing) {
-                enqueue_iteration<R, DIRECT, STATS>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev);
+                enqueue_iteration<R, DIRECT, STATS, ADJ>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev);
                 CUDA_CHECK(cudaGetLastError());
                 CUDA_CHECK(cudaEventSynchronize(kev[3]));
                 for (int k = 0; k < 3; k++) {
@@ -897,6 +1002,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
             CUDA_CHECK(cudaStreamSynchronize(stream));
             if (wv->h_ctr->error_flags & 1)
                 throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+            if (wv->h_ctr->error_flags & 2)
+                throw DeviceError("adjoint path longer than 16 surface vertices", NGI_ERR_UNSUPPORTED);
             if (wv->h_ctr->active == 0 && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples) break;
             if (iterations > max_iters) throw DeviceError("wave did not drain", NGI_ERR_DEVICE_TIMEOUT);
         }
@@ -944,7 +1051,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     cudaStream_t stream = user_stream ? user_stream : ds.stream;
     ds.last_stats = ngi_render_stats{};
     if (p.num_samples == 0) return;
-    int Q = p.wave_size > 0 ? p.wave_size : (1 << 21);
+    int Q = p.wave_size > 0 ? p.wave_size : (1 << 22);
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
@@ -961,6 +1068,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
@@ -1078,6 +1186,134 @@ void DeviceVisible(HostScene& hs, const double* h_pts, int64_t n, uint8_t* vis) 
         throw;
     }
     cleanup();
+}
+
+void DeviceUpdateTables(HostScene& hs) {
+    DeviceScene* ds = hs.dev;
+    if (!ds) return;
+    std::vector<DevMaterial<float>> mf; std::vector<DevLight<float>> lf; DevSensor<float> sf;
+    std::vector<DevMaterial<double>> md; std::vector<DevLight<double>> ld; DevSensor<double> sd;
+    std::vector<double> cdf; std::vector<float> epos, euv;
+    build_tables<float>(hs, mf, lf, sf, cdf, epos, euv);
+    build_tables<double>(hs, md, ld, sd, cdf, epos, euv);
+    CUDA_CHECK(cudaStreamSynchronize(ds->stream));
+    if (!mf.empty()) {
+        CUDA_CHECK(cudaMemcpy(ds->mats_f, mf.data(), mf.size() * sizeof(mf[0]), cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(ds->mats_d, md.data(), md.size() * sizeof(md[0]), cudaMemcpyHostToDevice));
+    }
+    if (!lf.empty()) {
+        CUDA_CHECK(cudaMemcpy(ds->lights_f, lf.data(), lf.size() * sizeof(lf[0]), cudaMemcpyHostToDevice));
+        CUDA_CHECK(cudaMemcpy(ds->lights_d, ld.data(), ld.size() * sizeof(ld[0]), cudaMemcpyHostToDevice));
+    }
+    std::memcpy(ds->sensor_f, &sf, sizeof(sf));
+    std::memcpy(ds->sensor_d, &sd, sizeof(sd));
+}
+
+namespace {
+
+template <typename R>
+void ensure_adjoint_buffers(RenderWave* wv, WaveView<R>& v) {
+    if (!wv->adjoint_buffers) {
+        auto A = [&](size_t bytes) -> void* {
+            void* p = nullptr;
+            CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+            wv->bufs.push_back(p);
+            return p;
+        };
+        v.pre = (uint4*)A(sizeof(uint4) * 2 * (size_t)wv->Q);
+        v.sh_pre = (uint4*)A(sizeof(uint4) * 4 * (size_t)wv->Q);
+        v.sh_info = (int2*)A(sizeof(int2) * 2 * (size_t)wv->Q);
+        wv->adjoint_buffers = true;
+    }
+}
+
+template <typename R, bool DIRECT>
+void run_backward(HostScene& hs, RenderWave* wv, WaveView<R>& v, const RenderConsts& rc, int ipg, cudaStream_t stream) {
+    ensure_adjoint_buffers(wv, v);
+    run_wave<R, DIRECT, false, true>(hs, wv, v, rc, ipg, false, stream);
+}
+
+}  // namespace
+
+void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const double* h_dfilm, double* grad_albedo,
+                          double* grad_emission) {
+    DeviceUpload(hs);
+    DeviceScene& ds = *hs.dev;
+    if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
+    if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
+        throw DeviceError("ptdirect needs at least one light", NGI_ERR_UNSUPPORTED);
+    if (p.max_num_vertices == -1 || p.max_num_vertices > kAdjMaxPrefix + 1)
+        throw DeviceError("the adjoint replays paths of at most 17 vertices: set max_num_vertices to 1..17",
+                          NGI_ERR_UNSUPPORTED);
+    if (hs.prims.size() > 65535) throw DeviceError("the adjoint supports at most 65535 primitives", NGI_ERR_UNSUPPORTED);
+    if (p.flags != 0) throw DeviceError("measurement flags are not available on the adjoint", NGI_ERR_INVALID_ARGUMENT);
+    const size_t np = hs.prims.size();
+    const size_t elems = 3 * (size_t)p.width * (size_t)p.height;
+    auto ensure = [&](double*& buf, size_t& have, size_t need) {
+        if (have < need) {
+            if (buf) cudaFree(buf);
+            buf = nullptr;
+            have = 0;
+            CUDA_CHECK(cudaMalloc(&buf, std::max<size_t>(need, 1) * sizeof(double)));
+            have = need;
+        }
+    };
+    ensure(ds.film, ds.film_elems, elems);
+    ensure(ds.adj, ds.adj_elems, elems);
+    ensure(ds.grads, ds.grad_elems, 6 * np);
+    cudaStream_t stream = ds.stream;
+    CUDA_CHECK(cudaMemsetAsync(ds.grads, 0, 6 * np * sizeof(double), stream));
+    ds.last_stats = ngi_render_stats{};
+    if (p.num_samples > 0) {
+        CUDA_CHECK(cudaMemsetAsync(ds.film, 0, elems * sizeof(double), stream));
+        CUDA_CHECK(cudaMemcpyAsync(ds.adj, h_dfilm, elems * sizeof(double), cudaMemcpyHostToDevice, stream));
+        // the film is normalised by W*H/N, so d(film)/d(raw contribution) = W*H/N
+        const double scale = (double)p.width * (double)p.height / (double)p.num_samples;
+        k_scale<<<grid_for((int)std::min<size_t>(elems, 1u << 30), 256), 256, 0, stream>>>(ds.adj, elems, scale);
+        CUDA_CHECK(cudaGetLastError());
+        int Q = p.wave_size > 0 ? p.wave_size : (1 << 22);
+        const long long need = std::max<long long>(p.num_samples, 256);
+        if ((long long)Q > need) Q = (int)need;
+        Q = (Q + 255) / 256 * 256;
+        RenderWave* wv = ensure_wave(ds, Q, p.precision);
+        RenderConsts rc{};
+        rc.renderer = p.renderer;
+        rc.max_vertices = p.max_num_vertices;
+        rc.num_samples = p.num_samples;
+        rc.sample_offset = p.sample_offset;
+        rc.seed = p.seed;
+        rc.width = p.width;
+        rc.height = p.height;
+        rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
+        const long long wh = (long long)p.width * p.height;
+        rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+        rc.trace_refill = p.trace_refill;
+    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
+        const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
+        const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
+        if (p.precision == NGI_PRECISION_FP64) {
+            WaveView<double>& v = wv->vd;
+            v.film = ds.film;
+            v.adj = ds.adj;
+            v.grad_albedo = ds.grads;
+            v.grad_emission = ds.grads + 3 * np;
+            if (direct) run_backward<double, true>(hs, wv, v, rc, ipg, stream);
+            else run_backward<double, false>(hs, wv, v, rc, ipg, stream);
+        } else {
+            WaveView<float>& v = wv->vf;
+            v.film = ds.film;
+            v.adj = ds.adj;
+            v.grad_albedo = ds.grads;
+            v.grad_emission = ds.grads + 3 * np;
+            if (direct) run_backward<float, true>(hs, wv, v, rc, ipg, stream);
+            else run_backward<float, false>(hs, wv, v, rc, ipg, stream);
+        }
+    }
+    std::vector<double> g(6 * np);
+    CUDA_CHECK(cudaMemcpyAsync(g.data(), ds.grads, 6 * np * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_CHECK(cudaStreamSynchronize(stream));
+    if (grad_albedo) std::memcpy(grad_albedo, g.data(), 3 * np * sizeof(double));
+    if (grad_emission) std::memcpy(grad_emission, g.data() + 3 * np, 3 * np * sizeof(double));
 }
 
 // ---- allocation-free render --------------------------------------------------------------------
@@ -1220,6 +1456,7 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
     if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v{};

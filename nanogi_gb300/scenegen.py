@@ -405,3 +405,53 @@ def sphere_field(num_spheres=40, grid=96, level=3, seed=11) -> SceneDesc:
 
 
 WORKLOADS.update({"material_box": material_box, "area_sensor_box": area_sensor_box, "sphere_field": sphere_field})
+
+
+def inverse_box(seed: int = 5, emitter_seed: int = 7) -> SceneDesc:
+    """The inverse-rendering workload: the Cornell box split into 64 diffuse material groups
+    (RGB albedo float32 U[0.05, 0.95], drawn with `seed`) lit by 2 ceiling quad emitters
+    (radiance U[5, 20], drawn with `emitter_seed`). Walls are cut into tiles: the back wall
+    4 x 4, the other four walls 3 x 3 each, plus the 12 faces of the two boxes = 64 groups."""
+    rng = np.random.default_rng(seed)
+    erng = np.random.default_rng(emitter_seed)
+    s = SceneDesc()
+    h = 1.0 - 1e-3
+    for i, (x0, x1) in enumerate([(0.2, 0.4), (0.6, 0.8)]):
+        le = erng.uniform(5.0, 20.0, 3)
+        t, p = area_light(le)
+        s.primitives.append(Primitive(t, p, quad((x0, h, 0.4), (x1, h, 0.4), (x1, h, 0.6), (x0, h, 0.6), (0, -1, 0)),
+                                      f"emitter{i}"))
+
+    def tiles(origin, eu, ev, n, normal, name):
+        o, eu, ev = np.asarray(origin, float), np.asarray(eu, float), np.asarray(ev, float)
+        out = []
+        for a in range(n):
+            for b in range(n):
+                p0 = o + eu * (a / n) + ev * (b / n)
+                p1 = o + eu * ((a + 1) / n) + ev * (b / n)
+                p2 = o + eu * ((a + 1) / n) + ev * ((b + 1) / n)
+                p3 = o + eu * (a / n) + ev * ((b + 1) / n)
+                out.append((quad(p0, p1, p2, p3, normal), f"{name}{a}{b}"))
+        return out
+
+    groups = []
+    groups += tiles((0, 0, 0), (1, 0, 0), (0, 1, 0), 4, (0, 0, 1), "back")
+    groups += tiles((0, 0, 1), (1, 0, 0), (0, 0, -1), 3, (0, 1, 0), "floor")
+    groups += tiles((0, 1, 0), (1, 0, 0), (0, 0, 1), 3, (0, -1, 0), "ceiling")
+    groups += tiles((0, 0, 0), (0, 1, 0), (0, 0, 1), 3, (1, 0, 0), "left")
+    groups += tiles((1, 0, 1), (0, 1, 0), (0, 0, -1), 3, (-1, 0, 0), "right")
+    for bi, b in enumerate([box((0.33, 0.3, 0.37), (0.3, 0.6, 0.3), 15.0), box((0.68, 0.15, 0.65), (0.3, 0.3, 0.3), -18.0)]):
+        for f in range(6):
+            idx = np.arange(4 * f, 4 * f + 4)
+            groups.append((Mesh(b.positions[idx].copy(), b.normals[idx].copy(), np.array([[0, 1, 2], [0, 2, 3]], np.int64)),
+                           f"box{bi}f{f}"))
+    assert len(groups) == 64
+    for m, name in groups:
+        r = rng.uniform(0.05, 0.95, 3).astype(np.float32).astype(np.float64)
+        t, p = diffuse(r)
+        s.primitives.append(Primitive(t, p, m, name))
+    s.primitives.append(pinhole((0.5, 0.5, 2.4), (0.5, 0.5, 0.0), (0, 1, 0), 36.0))
+    return s
+
+
+WORKLOADS["inverse_box"] = inverse_box

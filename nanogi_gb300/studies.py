@@ -1,6 +1,7 @@
 """Measurement studies beyond the throughput line of bench.py.
 
     python -m nanogi_gb300.studies convergence [--ref-spp 8192]
+    python -m nanogi_gb300.studies adjoint
 
 convergence: time to reach 1% relative RMSE against an FP64 reference, for the tuned path
 (FP32 shading) and the plain path (FP64 shading and path state), `pt` on the Cornell-box
@@ -86,14 +87,63 @@ def convergence(ref_spp: int = 8192, w: int = 256, h: int = 256, m: int = 8, max
     return out
 
 
+def adjoint_cost(w: int = 512, h: int = 512, spp: int = 64, m: int = 8, repeats: int = 3, descent_steps: int = 8):
+    """Inverse-rendering workload: time of the path-replay backward pass over the forward pass
+    (ptdirect, FP32 shading), plus a few steps of gradient descent on the L2 image loss."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    d = tempfile.mkdtemp(prefix="ngi_inverse_")
+    scene = ng.Scene.load(scenegen.write_scene(scenegen.inverse_box(seed=5, emitter_seed=7), d + "/a"), w / h)
+    hidden = ng.Scene.load(scenegen.write_scene(scenegen.inverse_box(seed=6, emitter_seed=8), d + "/b"), w / h)
+    ha, he = hidden.parameters()
+    hidden.close()
+    scene.build()
+    r = ng.Renderer(renderer="ptdirect", num_samples=w * h * spp, max_num_vertices=m, width=w, height=h, seed=3)
+    ta, te = scene.parameters()
+    scene.set_parameters(ha, he)
+    target = r.render(scene).copy()
+    scene.set_parameters(ta, te)
+    fwd, bwd = [], []
+    img = None
+    for _ in range(repeats + 1):
+        t0 = time.perf_counter()
+        img = r.render(scene)
+        fwd.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        r.backward(scene, 2.0 * (img - target))
+        bwd.append(time.perf_counter() - t0)
+    fwd, bwd = fwd[1:], bwd[1:]
+    mats = [i for i, p in enumerate(scene.parameters()[0]) if p.any()]
+    losses = []
+    a, e = ta.copy(), te.copy()
+    for step in range(descent_steps):
+        scene.set_parameters(a, e)
+        img = r.render(scene)
+        losses.append(float(((img - target) ** 2).sum()))
+        ga, ge = r.backward(scene, 2.0 * (img - target))
+        lr = 0.02 / max(np.abs(ga).max(), 1e-30)
+        a = np.clip(a - lr * ga, 0.0, 1.0)
+    scene.set_parameters(ta, te)
+    err0 = float(np.abs(ta[mats] - ha[mats]).mean())
+    err1 = float(np.abs(a[mats] - ha[mats]).mean())
+    scene.close()
+    return {"workload": f"inverse_box 64 diffuse groups + 2 emitters, {w}x{h}, ptdirect, {spp} spp, max length {m}",
+            "forward_seconds": float(np.median(fwd)), "backward_seconds": float(np.median(bwd)),
+            "grad_over_fwd": float(np.median(bwd) / np.median(fwd)), "descent_losses": losses,
+            "albedo_mean_abs_error_before": err0, "albedo_mean_abs_error_after": err1}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["convergence"])
+    ap.add_argument("study", choices=["convergence", "adjoint"])
     ap.add_argument("--ref-spp", type=int, default=8192)
     ap.add_argument("--max-ladder-spp", type=int, default=4096)
     a = ap.parse_args()
     if a.study == "convergence":
         print(json.dumps(convergence(a.ref_spp, max_ladder_spp=a.max_ladder_spp)), flush=True)
+    elif a.study == "adjoint":
+        print(json.dumps(adjoint_cost()), flush=True)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,203 @@
+"""GPU edge cases and statistical parity with the reference's own sampling (through the C ABI).
+
+* Statistical parity: the tuned FP32 GPU path (Philox, pixel-stratified) against the oracle in
+  reference mode (std::mt19937 per thread, uniform whole-image raster samples as in
+  rt.hpp:735). Same expectation, different random numbers: per-pixel Welch z-scores over
+  independent seeds must look like noise.
+* Edge cases the reference's loop structure implies: max vertices 1 and 2, sample counts
+  that are not a multiple of the pixel count, 1x1 films, empty scenes, sharded sample
+  ranges, wave sizes and graph lengths that must not change the result.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_rmse
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(path, aspect):
+    import nanogi_gb300 as ng
+
+    return ng.Scene.load(path, aspect)
+
+
+def _r(**kw):
+    import nanogi_gb300 as ng
+
+    return ng.Renderer(**kw)
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
+def test_statistical_parity_with_reference_sampling(native_lib, cornell, renderer):
+    from oracle.oracle import OracleScene
+
+    desc, path = cornell
+    W, H, spp, K = 16, 16, 64, 8
+    scene = _scene(path, W / H)
+    ora = OracleScene.from_desc(desc, W / H)
+    g = np.stack([_r(renderer=renderer, num_samples=W * H * spp, max_num_vertices=8, width=W, height=H,
+                     seed=100 + k).render(scene) for k in range(K)])
+    o = np.stack([ora.render(renderer, num_samples=W * H * spp, max_vertices=8, width=W, height=H, seed=200 + k,
+                             rng_mode="reference") for k in range(K)])
+    mg, mo = g.mean(0), o.mean(0)
+    se = np.sqrt(g.var(0, ddof=1) / K + o.var(0, ddof=1) / K)
+    ok = se > 0
+    z = (mg[ok] - mo[ok]) / se[ok]
+    assert abs(z.mean()) < 0.15, z.mean()
+    assert (np.abs(z) > 4.0).mean() < 0.01
+    # the whole image agrees far better than any single pixel
+    assert abs(mg.sum() / mo.sum() - 1) < 0.02
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
+def test_max_vertices_one_and_two(native_lib, cornell, renderer):
+    from oracle.oracle import OracleScene
+
+    desc, path = cornell
+    W, H = 12, 12
+    scene = _scene(path, W / H)
+    f1 = _r(renderer=renderer, num_samples=W * H * 4, max_num_vertices=1, width=W, height=H, seed=3).render(scene)
+    assert not f1.any()  # the loop ends before the first vertex does anything
+    f2 = _r(renderer=renderer, num_samples=W * H * 64, max_num_vertices=2, width=W, height=H, seed=3,
+            precision="fp64").render(scene)
+    ref = OracleScene.from_desc(desc, W / H).render(renderer, num_samples=W * H * 64, max_vertices=2, width=W,
+                                                    height=H, seed=3, rng_mode="replay", use_bvh=False)
+    assert rel_rmse(f2, ref) < 1e-9
+    assert f2.any()  # the light is visible from the camera
+
+
+@pytest.mark.parametrize("W,H,N", [(1, 1, 50), (3, 2, 7), (5, 4, 19), (8, 8, 64 * 3 + 5)])
+def test_odd_sizes_replay_the_oracle(native_lib, cornell, W, H, N):
+    from oracle.oracle import OracleScene
+
+    desc, path = cornell
+    scene = _scene(path, W / H)
+    for renderer in ("pt", "ptdirect"):
+        f = _r(renderer=renderer, num_samples=N, max_num_vertices=6, width=W, height=H, seed=9,
+               precision="fp64").render(scene)
+        ref = OracleScene.from_desc(desc, W / H).render(renderer, num_samples=N, max_vertices=6, width=W, height=H,
+                                                        seed=9, rng_mode="replay", use_bvh=False)
+        assert np.allclose(f, ref, rtol=1e-9, atol=1e-12), (renderer, W, H, N)
+
+
+def test_uniform_raster_mode_replays_the_oracle(native_lib, cornell):
+    from oracle.oracle import OracleScene
+
+    desc, path = cornell
+    W, H = 10, 10
+    scene = _scene(path, W / H)
+    f = _r(renderer="ptdirect", num_samples=W * H * 8, max_num_vertices=6, width=W, height=H, seed=4,
+           precision="fp64", raster="uniform").render(scene)
+    ref = OracleScene.from_desc(desc, W / H).render("ptdirect", num_samples=W * H * 8, max_vertices=6, width=W,
+                                                    height=H, seed=4, rng_mode="replay", raster="uniform",
+                                                    use_bvh=False)
+    assert np.allclose(f, ref, rtol=1e-9, atol=1e-12)
+
+
+def test_sample_ranges_add_up(native_lib, cornell):
+    """film(0..k) + film(k..N) = film(0..N) for k on a whole pass (raw sums)."""
+    desc, path = cornell
+    W, H = 8, 6
+    scene = _scene(path, W / H)
+    wh = W * H
+    N, k = wh * 10, wh * 4
+
+    def raw(off, n):
+        f = _r(renderer="ptdirect", num_samples=n, max_num_vertices=8, width=W, height=H, seed=21, sample_offset=off,
+               precision="fp64").render(scene)
+        return f * (n / wh)
+
+    whole = raw(0, N)
+    parts = raw(0, k) + raw(k, N - k)
+    assert np.allclose(parts, whole, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("knobs", [dict(wave_size=256), dict(wave_size=4096, iterations_per_graph=1),
+                                   dict(wave_size=1 << 20, iterations_per_graph=16), dict(trace_refill=1),
+                                   dict(trace_refill=32)])
+def test_launch_shape_does_not_change_the_film(native_lib, cornell, knobs):
+    desc, path = cornell
+    W, H = 16, 16
+    scene = _scene(path, W / H)
+    base = _r(renderer="ptdirect", num_samples=W * H * 16, max_num_vertices=8, width=W, height=H, seed=8).render(scene)
+    other = _r(renderer="ptdirect", num_samples=W * H * 16, max_num_vertices=8, width=W, height=H, seed=8,
+               **knobs).render(scene)
+    assert np.allclose(other, base, rtol=1e-9, atol=1e-12)
+
+
+def test_empty_and_lightless_scenes(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    s = scenegen.SceneDesc()
+    s.primitives.append(scenegen.pinhole((0, 0, 5), (0, 0, 0), (0, 1, 0), 40))
+    path = scenegen.write_scene(s, tmp_path / "empty")
+    scene = ng.Scene.load(path, 1.0)
+    f = _r(renderer="pt", num_samples=64, max_num_vertices=8, width=8, height=8).render(scene)
+    assert not f.any()
+    assert scene.info()["bvh_nodes"] == 0
+    with pytest.raises(ng.NanogiError) as e:
+        _r(renderer="ptdirect", num_samples=64, max_num_vertices=8, width=8, height=8).render(scene)
+    assert e.value.status == 7
+    # geometry but no light: pt renders black
+    c = scenegen.cornell_box()
+    c.primitives = [p for p in c.primitives if "L" not in p.type]
+    scene2 = ng.Scene.load(scenegen.write_scene(c, tmp_path / "dark"), 1.0)
+    f2 = _r(renderer="pt", num_samples=64 * 8, max_num_vertices=8, width=8, height=8).render(scene2)
+    assert not f2.any()
+
+
+def test_zero_samples_and_no_sensor(native_lib, tmp_path, cornell):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    _, path = cornell
+    scene = ng.Scene.load(path, 1.0)
+    f = _r(renderer="pt", num_samples=0, max_num_vertices=8, width=4, height=4).render(scene)
+    assert not f.any()
+    c = scenegen.cornell_box()
+    c.primitives = [p for p in c.primitives if "E" not in p.type]
+    s2 = ng.Scene.load(scenegen.write_scene(c, tmp_path / "nocam"), 1.0)
+    with pytest.raises(ng.NanogiError) as e:
+        _r(renderer="pt", num_samples=16, width=4, height=4).render(s2)
+    assert e.value.status == 1
+
+
+def test_area_sensor_replays_the_oracle(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    desc = scenegen.area_sensor_box()
+    W = H = 12
+    scene = ng.Scene.load(scenegen.write_scene(desc, tmp_path), 1.0)
+    for renderer in ("pt", "ptdirect"):
+        f = _r(renderer=renderer, num_samples=W * H * 16, max_num_vertices=-1, width=W, height=H, seed=25,
+               precision="fp64").render(scene)
+        ref = OracleScene.from_desc(desc, 1.0).render(renderer, num_samples=W * H * 16, max_vertices=-1, width=W,
+                                                      height=H, seed=25, rng_mode="replay", use_bvh=False)
+        assert rel_rmse(f, ref) < 1e-6, renderer
+
+
+def test_gpu_matches_committed_golden_films(native_lib, tmp_path):
+    """The plain FP64 GPU path reproduces the oracle's committed golden films."""
+    import json
+    from pathlib import Path
+
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    golden = Path(__file__).resolve().parent / "golden"
+    meta = json.loads((golden / "films.json").read_text())
+    for case in meta["cases"]:
+        desc = scenegen.WORKLOADS[case["scene"]]()
+        d = tmp_path / case["file"].replace(".npy", "")
+        scene = ng.Scene.load(scenegen.write_scene(desc, d), case["width"] / case["height"])
+        f = _r(renderer=case["renderer"], num_samples=case["num_samples"], max_num_vertices=case["max_vertices"],
+               width=case["width"], height=case["height"], seed=case["seed"], precision="fp64").render(scene)
+        ref = np.load(golden / case["file"])
+        assert rel_rmse(f, ref) < 1e-4, case["file"]
+        scene.close()
