@@ -248,7 +248,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
     return false;
 }
 
-constexpr int kPostponePct = 20;
+constexpr int kPostponePct = 0;  // measured fastest on the terrain workload: never postpone
 
 // Whole traversal of one ray (parity hooks and simple callers). Returns the leaf-order
 // triangle index of the nearest hit in [tmin, tmax) (ANY_HIT: of any hit) or -1; on a hit

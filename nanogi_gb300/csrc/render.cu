@@ -71,6 +71,7 @@ struct RenderConsts {
     long long strat_end;    // global sample indices below this are pixel-stratified
     int trace_refill;       // idle lanes that trigger a traversal warp's refill
     int trace_postpone;     // triangle-postponing threshold (percent of active lanes), -1 = default
+    int num_prims;          // primitives of the scene (adjoint gradient layout)
 };
 
 template <typename R>
@@ -176,18 +177,26 @@ NGI_D void prefix_set(uint4& a, uint4& b, int k, uint32_t prim) {
 // every sampling decision of pt/ptdirect is independent of the albedo R and the emission Le,
 // and C is a product holding R of each surface vertex on its path (the prefix, plus the
 // NEE vertex) and one Le, so dC/dR_m = C * n_m / R_m and dC/dLe = C / Le, channel by channel.
+//
+// The sums go to a per-block shared-memory accumulator when the scene is small enough
+// (smem != null: 6 floats per primitive, albedo then emission), flushed once per block by
+// adj_flush; otherwise straight to the FP64 global gradients.
 template <typename R>
 NGI_D void adj_accumulate(const WaveView<R>& w, const SceneView<R>& sv, uint32_t pixel, V3<R> C, const uint4& pa,
-                          const uint4& pb, int count, int vertex_prim, int light_prim) {
+                          const uint4& pb, int count, int vertex_prim, int light_prim, float* smem, int num_prims) {
     const double* a = w.adj + 3 * (size_t)pixel;
     const double wc[3] = {a[0] * (double)C.x, a[1] * (double)C.y, a[2] * (double)C.z};
     if (wc[0] == 0.0 && wc[1] == 0.0 && wc[2] == 0.0) return;
+    auto add = [&](int index, double v) {
+        if (smem) atomicAdd(smem + index, (float)v);
+        else atomicAdd(index < 3 * num_prims ? w.grad_albedo + index : w.grad_emission + (index - 3 * num_prims), v);
+    };
     auto add_albedo = [&](int m) {
         const V3<R> r = sv.mats[m].R_;
         const double rc[3] = {(double)r.x, (double)r.y, (double)r.z};
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            if (rc[c] != 0.0) atomicAdd(w.grad_albedo + 3 * (size_t)m + c, wc[c] / rc[c]);
+            if (rc[c] != 0.0) add(3 * m + c, wc[c] / rc[c]);
     };
     for (int k = 0; k < count; k++) add_albedo((int)prefix_get(pa, pb, k));
     if (vertex_prim >= 0) add_albedo(vertex_prim);
@@ -196,7 +205,26 @@ NGI_D void adj_accumulate(const WaveView<R>& w, const SceneView<R>& sv, uint32_t
         const double lc[3] = {(double)le.x, (double)le.y, (double)le.z};
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            if (lc[c] != 0.0) atomicAdd(w.grad_emission + 3 * (size_t)light_prim + c, wc[c] / lc[c]);
+            if (lc[c] != 0.0) add(3 * num_prims + 3 * light_prim + c, wc[c] / lc[c]);
+    }
+}
+
+// Largest scene (primitives) whose gradients fit the per-block shared-memory accumulator.
+constexpr int kAdjSmemPrims = 1024;
+
+NGI_D void adj_smem_clear(float* smem, int num_prims) {
+    if (!smem) return;
+    for (int i = threadIdx.x; i < 6 * num_prims; i += blockDim.x) smem[i] = 0.0f;
+    __syncthreads();
+}
+template <typename R>
+NGI_D void adj_flush(const WaveView<R>& w, float* smem, int num_prims) {
+    if (!smem) return;
+    __syncthreads();
+    for (int i = threadIdx.x; i < 6 * num_prims; i += blockDim.x) {
+        const float v = smem[i];
+        if (v != 0.0f)
+            atomicAdd(i < 3 * num_prims ? w.grad_albedo + i : w.grad_emission + (i - 3 * num_prims), (double)v);
     }
 }
 
@@ -274,6 +302,9 @@ NGI_D void store_ray(const WaveView<R>& w, int s, V3<R> o, V3<R> d) {
 
 template <typename R, bool DIRECT, bool ADJ>
 __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+    extern __shared__ float adj_smem[];
+    float* gsm = (ADJ && !DIRECT && rc.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
+    if (ADJ && !DIRECT) adj_smem_clear(gsm, rc.num_prims);
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
@@ -338,7 +369,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                             if (finite3(c)) {
                                 film_add(w.film, pixel, c);
                                 atomicAdd(&w.ctr->stat_contrib, 1ull);
-                                if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim);
+                                if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim, gsm, rc.num_prims);
                             } else {
                                 atomicAdd(&w.ctr->stat_nonfinite, 1ull);
                             }
@@ -517,6 +548,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
             if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
         }
     }
+    if (ADJ && !DIRECT) adj_flush(w, gsm, rc.num_prims);
 }
 
 // Adds a per-thread traversal count into a global counter with one atomic per warp.
@@ -534,7 +566,11 @@ NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
 // others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
 // and removes the tail of a fixed grid.
 template <typename R, bool SHADOW, bool STATS, bool ADJ = false>
-__global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone) {
+__global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone,
+                                                      int num_prims) {
+    extern __shared__ float adj_smem[];
+    float* gsm = (ADJ && num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
+    if (ADJ) adj_smem_clear(gsm, num_prims);
     const int n = SHADOW ? w.ctr->sh_count : w.ctr->ext_count;
     int* fetch = SHADOW ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
     TravState s;
@@ -591,7 +627,8 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                                     qa = w.sh_pre[2 * (size_t)item];
                                     qb = w.sh_pre[2 * (size_t)item + 1];
                                 }
-                                adj_accumulate(w, sv, pix, cc, qa, qb, count, (info.x >> 8) - 1, info.y);
+                                adj_accumulate(w, sv, pix, cc, qa, qb, count, (info.x >> 8) - 1, info.y, gsm,
+                                               num_prims);
                             }
                         } else {
                             atomicAdd(&w.ctr->stat_nonfinite, 1ull);
@@ -604,6 +641,7 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
             }
         }
     }
+    if (ADJ) adj_flush(w, gsm, num_prims);
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
     if (STATS) {
         warp_sum_add(SHADOW ? &w.ctr->sh_nodes : &w.ctr->ext_nodes, ts.nodes);
@@ -931,13 +969,14 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     const size_t len = offsetof(WaveCounters, error_flags) - off;
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
-    k_logic<R, DIRECT, ADJ><<<g_logic, 256, 0, stream>>>(sv, v, rc);
+    const size_t adj_bytes = (ADJ && rc.num_prims <= kAdjSmemPrims) ? 6 * sizeof(float) * rc.num_prims : 0;
+    k_logic<R, DIRECT, ADJ><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc);
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
     const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
-    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone);
+    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone, rc.num_prims);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_trace<R, true, STATS, ADJ><<<g_sh, kTraceBlock, 0, stream>>>(sv, v, refill, postpone);
+    k_trace<R, true, STATS, ADJ><<<g_sh, kTraceBlock, adj_bytes, stream>>>(sv, v, refill, postpone, rc.num_prims);
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
@@ -1068,6 +1107,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
@@ -1288,6 +1328,7 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
         const long long wh = (long long)p.width * p.height;
         rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
         rc.trace_refill = p.trace_refill;
+    rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
         const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
         const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
@@ -1456,6 +1497,7 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
     if (p.precision == NGI_PRECISION_FP64) {
