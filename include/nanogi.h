@@ -194,6 +194,39 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
 NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_params* params,
                                              double* d_film_rgb, void* stream);
 
+/* ---- batches (no counterpart in the reference: it renders one scene per process) ------ */
+
+typedef struct ngi_batch_options {
+    int32_t autotune;             /* 1: choose wave size, refill threshold and graph length by
+                                     short timed trials on a sample of every job first */
+    int32_t wave_size;            /* path slots; 0 = auto (the starting point of the autotuner) */
+    int32_t trace_refill;         /* 0 = auto */
+    int32_t iterations_per_graph; /* 0 = auto */
+    double autotune_fraction;     /* share of each job's samples per trial; 0 = 0.02 */
+} ngi_batch_options;
+
+typedef struct ngi_batch_stats {
+    double render_ms;             /* device time of the batch render (autotuning excluded) */
+    double autotune_ms;           /* device time of the autotuning trials */
+    int64_t samples;
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    int64_t iterations;
+    int32_t wave_size;            /* the configuration used */
+    int32_t trace_refill;
+    int32_t iterations_per_graph;
+    int32_t trials;
+} ngi_batch_stats;
+
+/* Renders num_jobs independent jobs -- scenes[i] with params[i] into the HOST film films[i]
+ * (width*height*3 doubles, normalised as ngi_render does) -- through ONE persistent wave of
+ * path slots replayed from one CUDA graph: every job's samples share the slots, so small
+ * jobs never leave the GPU idle. Jobs may differ in scene, renderer, resolution, samples,
+ * max vertices and seed; all must use the same precision. The same scene handle may appear
+ * in several jobs. films[i] may be NULL. stats may be NULL. */
+NGI_API ngi_status ngi_render_batch(ngi_scene* const* scenes, const ngi_render_params* params, int32_t num_jobs,
+                                    double* const* films, const ngi_batch_options* options, ngi_batch_stats* stats);
+
 /* ---- differentiable rendering (no counterpart in the reference) ---------------------- */
 
 /* Reads / replaces the differentiable parameters of every primitive: `albedo` is the R of

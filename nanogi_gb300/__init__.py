@@ -21,7 +21,7 @@ import numpy as np
 from . import capi
 from .capi import NanogiError, RenderParams, RenderStats, SceneInfo, check, load_library
 
-__all__ = ["Scene", "Renderer", "NanogiError", "save_image", "load_hdr", "load_library"]
+__all__ = ["Scene", "Renderer", "NanogiError", "render_batch", "save_image", "load_hdr", "load_library"]
 
 
 def _ptr(a: np.ndarray) -> ctypes.c_void_p:
@@ -193,6 +193,24 @@ class Renderer:
         check(load_library().ngi_render_device(scene.handle, ctypes.byref(p), ctypes.c_void_p(d_film_ptr),
                                                ctypes.c_void_p(stream)))
         self.last_stats = scene.last_stats()
+
+
+def render_batch(jobs, autotune: bool = False, wave_size: int = 0, trace_refill: int = 0,
+                 iterations_per_graph: int = 0, autotune_fraction: float = 0.0):
+    """Renders [(scene, Renderer), ...] in one persistent wave (ngi_render_batch).
+    Returns (films, stats): one (H, W, 3) film per job, normalised like Renderer.render."""
+    from .capi import BatchOptions, BatchStats
+
+    n = len(jobs)
+    scenes = (ctypes.c_void_p * n)(*[s.handle.value for s, _ in jobs])
+    params = (RenderParams * n)(*[r.params() for _, r in jobs])
+    films = [np.empty((r.height, r.width, 3), np.float64) for _, r in jobs]
+    ptrs = (ctypes.c_void_p * n)(*[f.ctypes.data for f in films])
+    opt = BatchOptions(autotune=int(autotune), wave_size=int(wave_size), trace_refill=int(trace_refill),
+                       iterations_per_graph=int(iterations_per_graph), autotune_fraction=float(autotune_fraction))
+    st = BatchStats()
+    check(load_library().ngi_render_batch(scenes, params, n, ptrs, ctypes.byref(opt), ctypes.byref(st)))
+    return films, {k: getattr(st, k) for k, _ in BatchStats._fields_}
 
 
 def save_image(path: str | os.PathLike, film: np.ndarray) -> None:

@@ -90,6 +90,31 @@ class SceneInfo(ctypes.Structure):
     ]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [
+        ("autotune", ctypes.c_int32),
+        ("wave_size", ctypes.c_int32),
+        ("trace_refill", ctypes.c_int32),
+        ("iterations_per_graph", ctypes.c_int32),
+        ("autotune_fraction", ctypes.c_double),
+    ]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [
+        ("render_ms", ctypes.c_double),
+        ("autotune_ms", ctypes.c_double),
+        ("samples", ctypes.c_int64),
+        ("extension_rays", ctypes.c_int64),
+        ("shadow_rays", ctypes.c_int64),
+        ("iterations", ctypes.c_int64),
+        ("wave_size", ctypes.c_int32),
+        ("trace_refill", ctypes.c_int32),
+        ("iterations_per_graph", ctypes.c_int32),
+        ("trials", ctypes.c_int32),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/nanogi.h declares
 _P = ctypes.POINTER
 PROTOTYPES = {
@@ -106,6 +131,8 @@ PROTOTYPES = {
     "ngi_get_render_stats": (ctypes.c_int, [ctypes.c_void_p, _P(RenderStats)]),
     "ngi_render_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p,
                                                  ctypes.c_void_p]),
+    "ngi_render_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                        _P(BatchOptions), _P(BatchStats)]),
     "ngi_scene_get_parameters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_scene_set_parameters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_render_backward": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p, ctypes.c_void_p,

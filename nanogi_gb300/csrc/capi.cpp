@@ -5,6 +5,7 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/nanogi.h"
 #include "device_scene.hpp"
@@ -189,6 +190,34 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
     }
     g_last_error.clear();
     return NGI_OK;
+}
+
+NGI_API ngi_status ngi_render_batch(ngi_scene* const* scenes, const ngi_render_params* params, int32_t num_jobs,
+                                    double* const* films, const ngi_batch_options* options, ngi_batch_stats* stats) {
+    if (num_jobs < 0 || (num_jobs > 0 && (!scenes || !params)))
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "bad job arrays");
+    std::vector<ngi::HostScene*> hs((size_t)num_jobs);
+    std::vector<ngi_render_params> ps((size_t)num_jobs);
+    for (int32_t j = 0; j < num_jobs; j++) {
+        const ngi_status st = CheckParams(scenes[j], &params[j]);
+        if (st != NGI_OK) return Fail(st, "job " + std::to_string(j) + ": " + g_last_error);
+        hs[(size_t)j] = scenes[j]->host.get();
+        ps[(size_t)j] = params[j];
+    }
+    ngi_batch_options opt{};
+    if (options) opt = *options;
+    if (opt.wave_size < 0 || opt.trace_refill < 0 || opt.trace_refill > 32 || opt.iterations_per_graph < 0 ||
+        opt.iterations_per_graph > 64 || !(opt.autotune_fraction >= 0.0) || opt.autotune_fraction > 1.0)
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "batch options out of range");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (num_jobs == 0) {
+        g_last_error.clear();
+        return NGI_OK;
+    }
+    return Guard([&]() {
+        ngi::DeviceRenderBatch(hs, ps, films, opt, stats);
+        return NGI_OK;
+    });
 }
 
 NGI_API ngi_status ngi_scene_get_parameters(const ngi_scene* scene, double* albedo, double* emission) {

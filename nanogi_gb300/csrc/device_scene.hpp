@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../include/nanogi.h"
 
@@ -82,6 +83,11 @@ void DeviceRenderNoAlloc(HostScene& scene, const ngi_render_params& params, doub
 // dLoss/dR (BSDF albedo) and dLoss/dLe per primitive from h_dfilm = dLoss/d(normalised film).
 void DeviceRenderBackward(HostScene& scene, const ngi_render_params& params, const double* h_dfilm,
                           double* grad_albedo, double* grad_emission);
+
+// Renders many independent jobs in one persistent wave (one CUDA graph), optionally after
+// autotuning the wave size / refill threshold / graph length on a sample of every job.
+void DeviceRenderBatch(std::vector<HostScene*>& scenes, const std::vector<ngi_render_params>& params,
+                       double* const* films, const ngi_batch_options& options, ngi_batch_stats* stats);
 
 // Pushes the host copy of the materials / lights (after a parameter update) to the device.
 void DeviceUpdateTables(HostScene& scene);

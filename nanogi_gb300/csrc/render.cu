@@ -74,6 +74,15 @@ struct RenderConsts {
     int num_prims;          // primitives of the scene (adjoint gradient layout)
 };
 
+// One job of a batch render: its scene, parameters, device film and first batch sample.
+template <typename R>
+struct JobView {
+    SceneView<R> sv;
+    RenderConsts rc;
+    double* film;
+    long long sample_base;
+};
+
 template <typename R>
 struct WaveView {
     int Q;
@@ -101,6 +110,9 @@ struct WaveView {
     const double* adj;       // dLoss/dfilm per pixel and channel, scaled by W*H/N
     double* grad_albedo;     // per primitive x 3
     double* grad_emission;   // per primitive x 3
+    // batches only (null otherwise)
+    int* job;                // per slot: job of the path
+    int* sh_job;             // per shadow ray: job of the ray
 };
 
 // Longest surface-vertex prefix the adjoint carries: paths of up to 17 vertices.
@@ -300,11 +312,14 @@ NGI_D void store_ray(const WaveView<R>& w, int s, V3<R> o, V3<R> d) {
     }
 }
 
-template <typename R, bool DIRECT, bool ADJ>
-__global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+// BATCH: every slot belongs to one job of a batch; its scene, parameters, film and renderer
+// come from the device job table (one persistent wave serves every job).
+template <typename R, bool DIRECT, bool ADJ, bool BATCH = false>
+__global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
+                                               const JobView<R>* __restrict__ jobs, int num_jobs) {
     extern __shared__ float adj_smem[];
-    float* gsm = (ADJ && !DIRECT && rc.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
-    if (ADJ && !DIRECT) adj_smem_clear(gsm, rc.num_prims);
+    float* gsm = (ADJ && !DIRECT && rc0.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
+    if (ADJ && !DIRECT) adj_smem_clear(gsm, rc0.num_prims);
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
@@ -315,6 +330,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
         sa.valid = false;
         uint4 pa = make_uint4(0u, 0u, 0u, 0u), pb = pa;  // adjoint: surface-vertex prefix of the path
         int sa_count = 0, sa_vprim = -1;
+        int job_a = 0, job_b = 0;  // batch job of the shadow rays of this slot
 
         if (st == SLOT_ACTIVE) {
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
@@ -322,6 +338,12 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
             const float4 h = w.hit[s];
             const int ti = __float_as_int(h.w);
             if (ti >= 0) {
+                const int job = BATCH ? w.job[s] : 0;
+                job_a = job;
+                const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
+                const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
+                double* const film = BATCH ? jobs[job].film : w.film;
+                const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
                 V3<R> o, d;
                 if (sizeof(R) == 8) {
                     const Vec4T<double> a = w.od_o[s], b = w.od_d[s];
@@ -361,13 +383,13 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                     pb = w.pre[2 * (size_t)s + 1];
                 }
 
-                if (!DIRECT && (mat.type & DT_L) && mat.l_type == LT_AREA) {
+                if (!direct && (mat.type & DT_L) && mat.l_type == LT_AREA) {
                     // Emission on a light hit (src/nanogi.cpp:568-575)
                     if (dot(g.sn, -d) > R(0)) {
                         const V3<R> c = thr * mat.Le;
                         if (!is_zero(c)) {
                             if (finite3(c)) {
-                                film_add(w.film, pixel, c);
+                                film_add(film, pixel, c);
                                 atomicAdd(&w.ctr->stat_contrib, 1ull);
                                 if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim, gsm, rc.num_prims);
                             } else {
@@ -384,7 +406,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                     if (!(rc.max_vertices != -1 && nv >= rc.max_vertices) && mat.bsdf != BSDF_NONE) {
                         tangent_space(g);
                         const V3<R> wi = -d;
-                        if (DIRECT) {
+                        if (direct) {
                             const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
                             next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
                             sa_count = nv - 2;
@@ -427,6 +449,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 w.sh_d[q] = make_float4(sa.dx, sa.dy, sa.dz, sa.tmax);
                 w.sh_c[q] = Vec4T<R>{sa.c.x, sa.c.y, sa.c.z, R(0)};
                 w.sh_pix[q] = sa.pixel;
+                if (BATCH) w.sh_job[q] = job_a;
                 if (ADJ) {
                     w.sh_pre[2 * (size_t)q] = pa;
                     w.sh_pre[2 * (size_t)q + 1] = pb;
@@ -449,7 +472,23 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 k = b + (unsigned long long)__popc(mask & lanemask_lt());
             }
             if (need_new) {
-                if (k >= (unsigned long long)rc.num_samples) {
+                int job = 0;
+                unsigned long long local = k;
+                if (BATCH && k < (unsigned long long)rc0.num_samples) {
+                    // job of batch sample k: last job whose first sample is <= k
+                    int lo = 0, hi = num_jobs - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if ((unsigned long long)jobs[mid].sample_base <= k) lo = mid; else hi = mid - 1;
+                    }
+                    job = lo;
+                    local = k - (unsigned long long)jobs[job].sample_base;
+                }
+                job_b = job;
+                const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
+                const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
+                const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
+                if (k >= (unsigned long long)rc0.num_samples) {
                     st = SLOT_DONE;
                 } else if (rc.max_vertices == 1) {
                     // the loop's first test ends the path before the sensor vertex does anything
@@ -457,7 +496,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                     st = SLOT_EMPTY;
                 } else {
                     // ---- sensor vertex (src/nanogi.cpp:450-479, 609-641) ----
-                    const unsigned long long gsample = (unsigned long long)rc.sample_offset + k;
+                    const unsigned long long gsample = (unsigned long long)rc.sample_offset + local;
                     const RngKey rk = make_rng(rc.seed, gsample);
                     Geom<R> ge;
                     V3<R> thr;
@@ -475,7 +514,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                         const R a = R(1) / cam.inv_area;
                         thr = v3<R>(a, a, a);
                     }
-                    if (DIRECT) {
+                    if (direct) {
                         const float4 un = rng4(rk, 1u, RNG_NEE_RR);
                         next_event(sv, rc, ge, true, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, 0u, un, sb);
                     }
@@ -516,6 +555,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                         w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
                         w.pixel[s] = pix;
                         w.sample[s] = gsample;
+                        if (BATCH) w.job[s] = job;
                         w.nverts[s] = 1;
                         want_ext = true;
                         st = SLOT_ACTIVE;
@@ -536,6 +576,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
                 w.sh_d[q] = make_float4(sb.dx, sb.dy, sb.dz, sb.tmax);
                 w.sh_c[q] = Vec4T<R>{sb.c.x, sb.c.y, sb.c.z, R(0)};
                 w.sh_pix[q] = sb.pixel;
+                if (BATCH) w.sh_job[q] = job_b;
                 if (ADJ) w.sh_info[q] = make_int2(0, sb.light_prim);  // sensor vertex: no surface factors
             }
         }
@@ -548,7 +589,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv, WaveView<R> w, R
             if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
         }
     }
-    if (ADJ && !DIRECT) adj_flush(w, gsm, rc.num_prims);
+    if (ADJ && !DIRECT) adj_flush(w, gsm, rc0.num_prims);
 }
 
 // Adds a per-thread traversal count into a global counter with one atomic per warp.
@@ -565,9 +606,9 @@ NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
 // the warp fetches that many new rays with one atomic and the lanes start them while the
 // others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
 // and removes the tail of a fixed grid.
-template <typename R, bool SHADOW, bool STATS, bool ADJ = false>
+template <typename R, bool SHADOW, bool STATS, bool ADJ = false, bool BATCH = false>
 __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone,
-                                                      int num_prims) {
+                                                      int num_prims, const JobView<R>* __restrict__ jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
     if (ADJ) adj_smem_clear(gsm, num_prims);
@@ -575,7 +616,10 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
     int* fetch = SHADOW ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
     TravState s;
     uint2 stack[kTraversalStack];
-    int item = -1, slot = -1;
+    int item = -1, slot = -1, job = 0;
+    const CwNode* nodes = sv.nodes;
+    const float4* tris = sv.tris;
+    int num_nodes = sv.num_nodes;
     bool exhausted = false;
     bool overflow = false;
     TraceStats ts{0u, 0u};
@@ -596,10 +640,17 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                     if (SHADOW) {
                         o = w.sh_o[i];
                         d = w.sh_d[i];
+                        if (BATCH) job = w.sh_job[i];
                     } else {
                         slot = w.ext_queue[i];
                         o = w.ray_o[slot];
                         d = w.ray_d[slot];
+                        if (BATCH) job = w.job[slot];
+                    }
+                    if (BATCH) {
+                        nodes = jobs[job].sv.nodes;
+                        tris = jobs[job].sv.tris;
+                        num_nodes = jobs[job].sv.num_nodes;
                     }
                     trav_init(s, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w);
                 }
@@ -608,8 +659,8 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
         const unsigned busy = __ballot_sync(0xFFFFFFFFu, item >= 0);
         if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
         if (item >= 0) {
-            const bool done = sv.num_nodes == 0 ||
-                              trav_step<SHADOW, STATS>(s, stack, sv.nodes, sv.tris, overflow, &ts, postpone);
+            const bool done = num_nodes == 0 ||
+                              trav_step<SHADOW, STATS>(s, stack, nodes, tris, overflow, &ts, postpone);
             if (done) {
                 if (SHADOW) {
                     if (s.hit < 0) {
@@ -617,7 +668,7 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                         const V3<R> cc = v3<R>(c.x, c.y, c.z);
                         if (finite3(cc)) {
                             const uint32_t pix = w.sh_pix[item];
-                            film_add(w.film, pix, cc);
+                            film_add(BATCH ? jobs[job].film : w.film, pix, cc);
                             atomicAdd(&w.ctr->stat_contrib, 1ull);
                             if (ADJ) {
                                 const int2 info = w.sh_info[item];
@@ -947,42 +998,45 @@ constexpr int kTraceBlock = 128;
 constexpr int kRefillLanes = 8;
 
 // Grid sizes of the persistent traversal kernels (queried once, outside any graph capture).
-template <typename R, bool STATS, bool ADJ = false>
+template <typename R, bool STATS, bool ADJ = false, bool BATCH = false>
 struct TraceGrids {
     static int ext() {
-        static const int g = persistent_grid(k_trace<R, false, STATS>, kTraceBlock);
+        static const int g = persistent_grid(k_trace<R, false, STATS, false, BATCH>, kTraceBlock);
         return g;
     }
     static int shadow() {
-        static const int g = persistent_grid(k_trace<R, true, STATS, ADJ>, kTraceBlock);
+        static const int g = persistent_grid(k_trace<R, true, STATS, ADJ, BATCH>, kTraceBlock);
         return g;
     }
 };
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
-                       int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev) {
+                       int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev,
+                       const JobView<R>* jobs = nullptr, int num_jobs = 0) {
     (void)g_trace;
-    const int g_ext = TraceGrids<R, STATS, ADJ>::ext();
-    const int g_sh = TraceGrids<R, STATS, ADJ>::shadow();
+    const int g_ext = TraceGrids<R, STATS, ADJ, BATCH>::ext();
+    const int g_sh = TraceGrids<R, STATS, ADJ, BATCH>::shadow();
     const size_t off = offsetof(WaveCounters, ext_count);
     const size_t len = offsetof(WaveCounters, error_flags) - off;
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
     const size_t adj_bytes = (ADJ && rc.num_prims <= kAdjSmemPrims) ? 6 * sizeof(float) * rc.num_prims : 0;
-    k_logic<R, DIRECT, ADJ><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc);
+    k_logic<R, DIRECT, ADJ, BATCH><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc, jobs, num_jobs);
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
     const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
-    k_trace<R, false, STATS><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone, rc.num_prims);
+    k_trace<R, false, STATS, false, BATCH><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone, rc.num_prims,
+                                                                             jobs);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_trace<R, true, STATS, ADJ><<<g_sh, kTraceBlock, adj_bytes, stream>>>(sv, v, refill, postpone, rc.num_prims);
+    k_trace<R, true, STATS, ADJ, BATCH><<<g_sh, kTraceBlock, adj_bytes, stream>>>(sv, v, refill, postpone,
+                                                                                 rc.num_prims, jobs);
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
-              bool kernel_timing, cudaStream_t stream) {
+              bool kernel_timing, cudaStream_t stream, const JobView<R>* jobs = nullptr, int num_jobs = 0) {
     DeviceScene& ds = *hs.dev;
     const SceneView<R> sv = make_view<R>(ds);
     const int g_logic = grid_for(v.Q, 256);
@@ -991,14 +1045,15 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
 
-    TraceGrids<R, STATS, ADJ>::ext();
-    TraceGrids<R, STATS, ADJ>::shadow();
+    TraceGrids<R, STATS, ADJ, BATCH>::ext();
+    TraceGrids<R, STATS, ADJ, BATCH>::shadow();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < iters_per_graph; it++)
-            enqueue_iteration<R, DIRECT, STATS, ADJ>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr);
+            enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr, jobs,
+                                                            num_jobs);
         const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
         if (cap != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
@@ -1023,7 +1078,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
         while (true) {
             if (kernel_timing) {
-                enqueue_iteration<R, DIRECT, STATS, ADJ>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev);
+                enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev, jobs,
+                                                                num_jobs);
                 CUDA_CHECK(cudaGetLastError());
                 CUDA_CHECK(cudaEventSynchronize(kev[3]));
                 for (int k = 0; k < 3; k++) {
@@ -1355,6 +1411,224 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
     CUDA_CHECK(cudaStreamSynchronize(stream));
     if (grad_albedo) std::memcpy(grad_albedo, g.data(), 3 * np * sizeof(double));
     if (grad_emission) std::memcpy(grad_emission, g.data() + 3 * np, 3 * np * sizeof(double));
+}
+
+// ---- batches ----------------------------------------------------------------------------------
+namespace {
+
+template <typename R>
+void ensure_batch_buffers(RenderWave* wv, WaveView<R>& v) {
+    if (!v.job) {
+        void* a = nullptr;
+        void* b = nullptr;
+        CUDA_CHECK(cudaMalloc(&a, sizeof(int) * (size_t)wv->Q));
+        wv->bufs.push_back(a);
+        CUDA_CHECK(cudaMalloc(&b, sizeof(int) * 2 * (size_t)wv->Q));
+        wv->bufs.push_back(b);
+        v.job = (int*)a;
+        v.sh_job = (int*)b;
+    }
+}
+
+RenderConsts consts_of(const ngi_render_params& p, int num_prims) {
+    RenderConsts rc{};
+    rc.renderer = p.renderer;
+    rc.max_vertices = p.max_num_vertices;
+    rc.num_samples = p.num_samples;
+    rc.sample_offset = p.sample_offset;
+    rc.seed = p.seed;
+    rc.width = p.width;
+    rc.height = p.height;
+    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
+    const long long wh = (long long)p.width * p.height;
+    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    rc.trace_refill = p.trace_refill;
+    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
+    rc.num_prims = num_prims;
+    return rc;
+}
+
+struct BatchConfig {
+    int wave, refill, ipg;
+};
+
+// One batch render of `jobs` (job tables already filled but for films / sample bases);
+// returns the device milliseconds of the wave.
+template <typename R>
+double batch_pass(std::vector<HostScene*>& scenes, const std::vector<ngi_render_params>& params,
+                  const std::vector<long long>& samples, double* d_films, const std::vector<size_t>& film_off,
+                  const BatchConfig& cfg, int precision, cudaStream_t stream, ngi_batch_stats* st) {
+    HostScene& hs0 = *scenes[0];
+    DeviceScene& ds0 = *hs0.dev;
+    const int n = (int)scenes.size();
+    std::vector<JobView<R>> jv(n);
+    long long total = 0;
+    int max_vertices = 1;
+    bool unbounded = false;
+    for (int j = 0; j < n; j++) {
+        jv[j].sv = make_view<R>(*scenes[j]->dev);
+        ngi_render_params p = params[j];
+        p.num_samples = samples[j];
+        jv[j].rc = consts_of(p, (int)scenes[j]->prims.size());
+        jv[j].film = d_films + film_off[j];
+        jv[j].sample_base = total;
+        total += samples[j];
+        if (p.max_num_vertices == -1) unbounded = true;
+        max_vertices = std::max(max_vertices, p.max_num_vertices);
+    }
+    JobView<R>* d_jobs = nullptr;
+    CUDA_CHECK(cudaMalloc(&d_jobs, sizeof(JobView<R>) * n));
+    double ms = 0;
+    try {
+        CUDA_CHECK(cudaMemcpyAsync(d_jobs, jv.data(), sizeof(JobView<R>) * n, cudaMemcpyHostToDevice, stream));
+        long long need = std::max<long long>(total, 256);
+        int Q = (int)std::min<long long>(cfg.wave, need);
+        Q = (Q + 255) / 256 * 256;
+        RenderWave* wv = ensure_wave(ds0, Q, precision);
+        WaveView<R>& v = precision == NGI_PRECISION_FP64 ? *(WaveView<R>*)&wv->vd : *(WaveView<R>*)&wv->vf;
+        ensure_batch_buffers(wv, v);
+        RenderConsts rc0 = consts_of(params[0], 0);
+        rc0.num_samples = total;
+        rc0.max_vertices = unbounded ? -1 : max_vertices;
+        rc0.trace_refill = cfg.refill;
+        rc0.trace_postpone = -1;
+        WaveView<R> vv = v;
+        vv.film = d_films;
+        if (total > 0) run_wave<R, false, false, false, true>(hs0, wv, vv, rc0, cfg.ipg, false, stream, d_jobs, n);
+        ms = ds0.last_stats.render_ms;
+        if (st) {
+            st->samples = total;
+            st->extension_rays = ds0.last_stats.extension_rays;
+            st->shadow_rays = ds0.last_stats.shadow_rays;
+            st->iterations = ds0.last_stats.iterations;
+        }
+    } catch (...) {
+        cudaStreamSynchronize(stream);
+        cudaFree(d_jobs);
+        throw;
+    }
+    CUDA_CHECK(cudaStreamSynchronize(stream));
+    cudaFree(d_jobs);
+    return ms;
+}
+
+template <typename R>
+void render_batch(std::vector<HostScene*>& scenes, const std::vector<ngi_render_params>& params, double* const* films,
+                  const ngi_batch_options& opt, ngi_batch_stats* stats) {
+    const int n = (int)scenes.size();
+    const int precision = params[0].precision;
+    DeviceScene& ds0 = *scenes[0]->dev;
+    cudaStream_t stream = ds0.stream;
+    std::vector<size_t> film_off(n + 1, 0);
+    for (int j = 0; j < n; j++) film_off[j + 1] = film_off[j] + 3 * (size_t)params[j].width * params[j].height;
+    double* d_films = nullptr;
+    CUDA_CHECK(cudaMalloc(&d_films, std::max<size_t>(film_off[n], 1) * sizeof(double)));
+    try {
+        BatchConfig cfg{opt.wave_size > 0 ? opt.wave_size : (1 << 22), opt.trace_refill > 0 ? opt.trace_refill : kRefillLanes,
+                        opt.iterations_per_graph > 0 ? opt.iterations_per_graph : 4};
+        double tune_ms = 0;
+        int trials = 0;
+        if (opt.autotune) {
+            // Coordinate search over wave size, refill threshold and graph length on a sample of
+            // every job (the trials render into the films, which are cleared afterwards).
+            const double frac = opt.autotune_fraction > 0 ? opt.autotune_fraction : 0.02;
+            std::vector<long long> trial(n);
+            long long trial_total = 0;
+            for (int j = 0; j < n; j++) {
+                const long long wh = (long long)params[j].width * params[j].height;
+                trial[j] = std::min<long long>(params[j].num_samples,
+                                               std::max<long long>(wh, (long long)(params[j].num_samples * frac)));
+                trial_total += trial[j];
+            }
+            auto measure = [&](const BatchConfig& c) {
+                CUDA_CHECK(cudaMemsetAsync(d_films, 0, film_off[n] * sizeof(double), stream));
+                const double ms = batch_pass<R>(scenes, params, trial, d_films, film_off, c, precision, stream, nullptr);
+                tune_ms += ms;
+                trials++;
+                return ms;
+            };
+            measure(cfg);  // warm: kernels, graphs, wave allocation
+            double best = measure(cfg);
+            const int waves[] = {1 << 20, 1 << 21, 1 << 22};
+            for (int wv : waves) {
+                if (wv == cfg.wave || wv > std::max<long long>(trial_total, 256) * 2) continue;
+                BatchConfig c = cfg;
+                c.wave = wv;
+                const double ms = measure(c);
+                if (ms < best) { best = ms; cfg = c; }
+            }
+            const int refills[] = {4, 8, 12, 16};
+            for (int r : refills) {
+                if (r == cfg.refill) continue;
+                BatchConfig c = cfg;
+                c.refill = r;
+                const double ms = measure(c);
+                if (ms < best) { best = ms; cfg = c; }
+            }
+            const int ipgs[] = {2, 4, 8};
+            for (int g : ipgs) {
+                if (g == cfg.ipg) continue;
+                BatchConfig c = cfg;
+                c.ipg = g;
+                const double ms = measure(c);
+                if (ms < best) { best = ms; cfg = c; }
+            }
+        }
+        CUDA_CHECK(cudaMemsetAsync(d_films, 0, film_off[n] * sizeof(double), stream));
+        std::vector<long long> samples(n);
+        for (int j = 0; j < n; j++) samples[j] = params[j].num_samples;
+        ngi_batch_stats st{};
+        const double ms = batch_pass<R>(scenes, params, samples, d_films, film_off, cfg, precision, stream, &st);
+        for (int j = 0; j < n; j++) {
+            const size_t elems = film_off[j + 1] - film_off[j];
+            if (params[j].num_samples > 0) {
+                const double scale = (double)params[j].width * (double)params[j].height / (double)params[j].num_samples;
+                k_scale<<<grid_for((int)std::min<size_t>(elems, 1u << 30), 256), 256, 0, stream>>>(d_films + film_off[j],
+                                                                                                 elems, scale);
+                CUDA_CHECK(cudaGetLastError());
+            }
+            if (films[j])
+                CUDA_CHECK(cudaMemcpyAsync(films[j], d_films + film_off[j], elems * sizeof(double),
+                                           cudaMemcpyDeviceToHost, stream));
+        }
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        if (stats) {
+            *stats = st;
+            stats->render_ms = ms;
+            stats->autotune_ms = tune_ms;
+            stats->trials = trials;
+            stats->wave_size = cfg.wave;
+            stats->trace_refill = cfg.refill;
+            stats->iterations_per_graph = cfg.ipg;
+        }
+    } catch (...) {
+        cudaStreamSynchronize(stream);
+        cudaFree(d_films);
+        throw;
+    }
+    cudaFree(d_films);
+}
+
+}  // namespace
+
+void DeviceRenderBatch(std::vector<HostScene*>& scenes, const std::vector<ngi_render_params>& params,
+                       double* const* films, const ngi_batch_options& opt, ngi_batch_stats* stats) {
+    if (scenes.empty()) return;
+    for (size_t j = 0; j < scenes.size(); j++) {
+        DeviceUpload(*scenes[j]);
+        const ngi_render_params& p = params[j];
+        if (scenes[j]->sensor_prim < 0)
+            throw DeviceError("job " + std::to_string(j) + ": the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
+        if (p.renderer == NGI_RENDERER_PTDIRECT && scenes[j]->dev->num_lights == 0)
+            throw DeviceError("job " + std::to_string(j) + ": ptdirect needs at least one light", NGI_ERR_UNSUPPORTED);
+        if (p.precision != params[0].precision)
+            throw DeviceError("every job of a batch must use the same precision", NGI_ERR_INVALID_ARGUMENT);
+        if (p.flags != 0) throw DeviceError("measurement flags are not available on batches", NGI_ERR_INVALID_ARGUMENT);
+        if (scenes[j]->dev->device != scenes[0]->dev->device)
+            throw DeviceError("every scene of a batch must live on the same device", NGI_ERR_INVALID_ARGUMENT);
+    }
+    if (params[0].precision == NGI_PRECISION_FP64) render_batch<double>(scenes, params, films, opt, stats);
+    else render_batch<float>(scenes, params, films, opt, stats);
 }
 
 // ---- allocation-free render --------------------------------------------------------------------

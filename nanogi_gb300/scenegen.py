@@ -455,3 +455,104 @@ def inverse_box(seed: int = 5, emitter_seed: int = 7) -> SceneDesc:
 
 
 WORKLOADS["inverse_box"] = inverse_box
+
+
+def batch_jobs(num_jobs: int = 256, seed: int = 1000, pool_size: int = 160, max_tris: int = 200_000):
+    """The batched-render workload: `num_jobs` independent jobs, each with a resolution drawn
+    uniformly from {64^2, 128^2, 256^2, 512^2}, a triangle count log-uniform in 1k..max_tris,
+    spp log-uniform 16..1024, max path length uniform 4..24 and the terrain workload's material
+    distribution. Each job's clutter is a random subset (seeded per job: seed + job index) of a
+    shared pool of icospheres (levels 1-4) and boxes, plus a floor, 1-2 quad lights and a camera.
+
+    Returns (primitives of the pool, list of job dicts) -- pass them to write_batch()."""
+    prng = np.random.default_rng(seed - 1)
+    pool = []
+    for i in range(pool_size):
+        kind = prng.integers(0, 5)
+        c = prng.uniform(-4, 4, 3) * np.array([1.0, 0.0, 1.0]) + np.array([0.0, 0.0, 0.0])
+        if kind < 4:
+            level = int(kind) + 1
+            r = float(np.exp(prng.uniform(np.log(0.15), np.log(0.8))))
+            c[1] = r
+            mesh = sphere_mesh(c, r, level)
+        else:
+            sz = prng.uniform(0.2, 1.2, 3)
+            c[1] = sz[1] / 2
+            mesh = box(c, sz, float(prng.uniform(-45, 45)))
+        k = int(prng.integers(0, 4))
+        if k == 0:
+            t, p = diffuse(prng.uniform(0.1, 0.9, 3))
+        elif k == 1:
+            t, p = glossy(prng.uniform(0.5, 1.0, 3), phong_to_beckmann(float(np.exp(prng.uniform(np.log(10), np.log(1000))))))
+        elif k == 2:
+            t, p = mirror((0.95, 0.95, 0.95))
+        else:
+            t, p = glass(1.5)
+        pool.append(Primitive(t, p, mesh, f"pool{i}"))
+    sizes = np.array([len(p.mesh.faces) for p in pool])
+    jobs = []
+    for j in range(num_jobs):
+        rng = np.random.default_rng(seed + j)
+        res = int(rng.choice([64, 128, 256, 512]))
+        target = int(np.exp(rng.uniform(np.log(1000), np.log(max_tris))))
+        spp = int(np.exp(rng.uniform(np.log(16), np.log(1024))))
+        m = int(rng.integers(4, 25))
+        order = rng.permutation(pool_size)
+        chosen, total = [], 0
+        for i in order:
+            if total >= target:
+                break
+            if total + sizes[i] > 1.5 * target and total > 0:
+                continue
+            chosen.append(int(i))
+            total += int(sizes[i])
+        nl = int(rng.integers(1, 3))
+        lights = [(rng.uniform(-3, 3), rng.uniform(-3, 3), rng.uniform(5.0, 20.0, 3)) for _ in range(nl)]
+        ang = rng.uniform(0, 2 * np.pi)
+        eye = (9.0 * np.cos(ang), rng.uniform(3.0, 6.0), 9.0 * np.sin(ang))
+        jobs.append({"res": res, "spp": spp, "max_vertices": m, "pool": chosen, "triangles": total + 2 + 2 * nl,
+                     "lights": lights, "eye": eye, "renderer": "ptdirect", "seed": seed + j})
+    return pool, jobs
+
+
+def write_batch(pool, jobs, directory) -> list:
+    """Writes the pool's OBJ files once and one YAML per job; returns the YAML paths."""
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    files = []
+    for i, p in enumerate(pool):
+        fn = f"pool_{i:04d}.obj"
+        if not (d / fn).exists():
+            write_obj(d / fn, p.mesh, p.name)
+        files.append(fn)
+    floor = quad((-6, 0, 6), (6, 0, 6), (6, 0, -6), (-6, 0, -6), (0, 1, 0))
+    if not (d / "floor.obj").exists():
+        write_obj(d / "floor.obj", floor, "floor")
+    paths = []
+    for j, job in enumerate(jobs):
+        lines = ["version: 5", "scene:", "  primitives:"]
+
+        def add(type_list, params, mesh_file):
+            lines.append(f"    - type: [{', '.join(type_list)}]")
+            if mesh_file:
+                lines.append("      mesh:")
+                lines.append(f"        path: '{mesh_file}'")
+            lines.append("      params:")
+            lines.append(_yaml_value(params, 8).rstrip("\n"))
+
+        for k, (lx, lz, le) in enumerate(job["lights"]):
+            fn = f"light_{j:04d}_{k}.obj"
+            write_obj(d / fn, quad((lx - 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz + 0.7),
+                                   (lx - 0.7, 6.0, lz + 0.7), (0, -1, 0)), "light")
+            t, p = area_light(le)
+            add(t, p, fn)
+        t, p = diffuse((0.5, 0.5, 0.5))
+        add(t, p, "floor.obj")
+        for i in job["pool"]:
+            add(pool[i].type, pool[i].params, files[i])
+        cam = pinhole(job["eye"], (0.0, 0.5, 0.0), (0, 1, 0), 50.0)
+        add(cam.type, cam.params, None)
+        path = d / f"job_{j:04d}.yml"
+        path.write_text("\n".join(lines) + "\n")
+        paths.append(path)
+    return paths

@@ -2,6 +2,7 @@
 
     python -m nanogi_gb300.studies convergence [--ref-spp 8192]
     python -m nanogi_gb300.studies adjoint
+    python -m nanogi_gb300.studies batch
 
 convergence: time to reach 1% relative RMSE against an FP64 reference, for the tuned path
 (FP32 shading) and the plain path (FP64 shading and path state), `pt` on the Cornell-box
@@ -134,9 +135,54 @@ def adjoint_cost(w: int = 512, h: int = 512, spp: int = 64, m: int = 8, repeats:
             "albedo_mean_abs_error_before": err0, "albedo_mean_abs_error_after": err1}
 
 
+def batch(num_jobs: int = 256):
+    """Batched renders: `num_jobs` independent jobs (the batch workload of scenegen.batch_jobs)
+    through one persistent wave replayed from one CUDA graph, after autotuning, against the
+    same jobs rendered one after another through ngi_render."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    pool, jobs = scenegen.batch_jobs(num_jobs=num_jobs)
+    d = tempfile.mkdtemp(prefix="ngi_batch_")
+    paths = scenegen.write_batch(pool, jobs, d)
+    t0 = time.perf_counter()
+    scenes = [ng.Scene.load(p, 1.0) for p in paths]
+    for sc in scenes:
+        sc.build()
+    load_s = time.perf_counter() - t0
+    work = [(sc, ng.Renderer(renderer=j["renderer"], num_samples=j["res"] * j["res"] * j["spp"],
+                             max_num_vertices=j["max_vertices"], width=j["res"], height=j["res"], seed=j["seed"]))
+            for sc, j in zip(scenes, jobs)]
+    ng.render_batch(work[:8])  # warm the batch kernels
+    t0 = time.perf_counter()
+    films, st = ng.render_batch(work, autotune=True)
+    batch_wall = time.perf_counter() - t0
+    rays = st["extension_rays"] + st["shadow_rays"]
+    seq_ms, seq_rays = 0.0, 0
+    t0 = time.perf_counter()
+    for sc, r in work:
+        r.render(sc)
+        seq_ms += r.last_stats["render_ms"]
+        seq_rays += r.last_stats["extension_rays"] + r.last_stats["shadow_rays"]
+    seq_wall = time.perf_counter() - t0
+    out = {"workload": f"{num_jobs} jobs, res {{64,128,256,512}}^2, tris log-U[1k,200k] "
+                       f"(mean {np.mean([j['triangles'] for j in jobs]):.0f}), spp log-U[16,1024], max length U[4,24], ptdirect",
+           "samples": st["samples"], "load_and_build_seconds": load_s,
+           "batch": {"device_ms": st["render_ms"], "wall_seconds": batch_wall, "autotune_ms": st["autotune_ms"],
+                     "trials": st["trials"], "mrays_per_s": rays / (st["render_ms"] / 1e3) / 1e6,
+                     "msamples_per_s": st["samples"] / (st["render_ms"] / 1e3) / 1e6,
+                     "config": {"wave_size": st["wave_size"], "trace_refill": st["trace_refill"],
+                                "iterations_per_graph": st["iterations_per_graph"]}},
+           "one_by_one": {"device_ms": seq_ms, "wall_seconds": seq_wall, "mrays_per_s": seq_rays / (seq_ms / 1e3) / 1e6},
+           "speedup_device": seq_ms / st["render_ms"], "speedup_wall": seq_wall / batch_wall}
+    for sc in scenes:
+        sc.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["convergence", "adjoint"])
+    ap.add_argument("study", choices=["convergence", "adjoint", "batch"])
     ap.add_argument("--ref-spp", type=int, default=8192)
     ap.add_argument("--max-ladder-spp", type=int, default=4096)
     a = ap.parse_args()
@@ -144,6 +190,8 @@ def main():
         print(json.dumps(convergence(a.ref_spp, max_ladder_spp=a.max_ladder_spp)), flush=True)
     elif a.study == "adjoint":
         print(json.dumps(adjoint_cost()), flush=True)
+    elif a.study == "batch":
+        print(json.dumps(batch()), flush=True)
 
 
 if __name__ == "__main__":

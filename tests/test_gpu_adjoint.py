@@ -175,8 +175,9 @@ def test_torch_autograd_wrapper(inverse_setup):
     scene.set_parameters(ta, te)
     img = r.render(scene)
     ga, ge = r.backward(scene, 2.0 * (img - target.numpy()))
-    assert np.allclose(a.grad.numpy(), ga, rtol=1e-9, atol=1e-12)
-    assert np.allclose(e.grad.numpy(), ge, rtol=1e-9, atol=1e-12)
+    # gradients are summed per block in FP32 in atomic order: two replays agree to ~1e-6
+    assert np.allclose(a.grad.numpy(), ga, rtol=1e-4, atol=1e-6 * np.abs(ga).max())
+    assert np.allclose(e.grad.numpy(), ge, rtol=1e-4, atol=1e-6 * np.abs(ge).max())
     # one gradient step lowers the loss
     with torch.no_grad():
         a2 = (a - 1e-4 * a.grad / a.grad.abs().max()).clamp(0.0, 1.0)

@@ -1,0 +1,86 @@
+"""Batched renders (ngi_render_batch): many independent jobs through one persistent wave.
+
+Every job of a batch must produce the film it produces when rendered alone with the same
+parameters (same Philox paths; only the FP64 summation order differs), whatever the mix of
+scenes, renderers, resolutions, sample counts and path lengths, with and without the
+autotuner.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch_scenes(native_lib, tmp_path_factory):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    pool, jobs = scenegen.batch_jobs(num_jobs=10, seed=2000, pool_size=40, max_tris=20_000)
+    paths = scenegen.write_batch(pool, jobs, tmp_path_factory.mktemp("batch"))
+    scenes = [ng.Scene.load(p, 1.0) for p in paths]
+    cornell = ng.Scene.load(scenegen.write_scene(scenegen.cornell_box(), tmp_path_factory.mktemp("cb")), 1.0)
+    yield scenes, jobs, cornell
+    for s in scenes:
+        s.close()
+    cornell.close()
+
+
+def _jobs(batch_scenes, scale=1):
+    import nanogi_gb300 as ng
+
+    scenes, jobs, cornell = batch_scenes
+    out = []
+    for k, (s, j) in enumerate(zip(scenes, jobs)):
+        res = max(8, j["res"] // 8)
+        spp = max(1, j["spp"] // 16) * scale
+        out.append((s, ng.Renderer(renderer="pt" if k % 3 == 0 else "ptdirect", num_samples=res * res * spp + k,
+                                   max_num_vertices=j["max_vertices"], width=res, height=res, seed=j["seed"])))
+    # the same scene twice, different resolutions / renderers
+    out.append((cornell, ng.Renderer(renderer="pt", num_samples=16 * 12 * 40, max_num_vertices=8, width=16, height=12,
+                                     seed=5)))
+    out.append((cornell, ng.Renderer(renderer="ptdirect", num_samples=24 * 24 * 8, max_num_vertices=-1, width=24,
+                                     height=24, seed=6)))
+    return out
+
+
+@pytest.mark.parametrize("autotune", [False, True])
+def test_batch_equals_individual_renders(batch_scenes, autotune):
+    import nanogi_gb300 as ng
+
+    jobs = _jobs(batch_scenes)
+    films, st = ng.render_batch(jobs, autotune=autotune, autotune_fraction=0.05)
+    assert st["samples"] == sum(r.num_samples for _, r in jobs)
+    if autotune:
+        assert st["trials"] >= 3
+    for (scene, r), f in zip(jobs, films):
+        ref = r.render(scene)
+        assert np.allclose(f, ref, rtol=1e-9, atol=1e-12), (r.renderer, r.width, r.num_samples)
+
+
+def test_batch_small_wave_and_options(batch_scenes):
+    import nanogi_gb300 as ng
+
+    jobs = _jobs(batch_scenes)[:4]
+    films, st = ng.render_batch(jobs, wave_size=512, trace_refill=4, iterations_per_graph=2)
+    assert st["wave_size"] == 512 and st["trace_refill"] == 4 and st["iterations_per_graph"] == 2
+    for (scene, r), f in zip(jobs, films):
+        assert np.allclose(f, r.render(scene), rtol=1e-9, atol=1e-12)
+
+
+def test_batch_rejects_mixed_precision_and_bad_jobs(batch_scenes):
+    import nanogi_gb300 as ng
+
+    jobs = _jobs(batch_scenes)[:2]
+    jobs[1][1].precision = "fp64"
+    with pytest.raises(ng.NanogiError):
+        ng.render_batch(jobs)
+    jobs[1][1].precision = "fp32"
+    jobs[1][1].width = 0
+    with pytest.raises(ng.NanogiError) as e:
+        ng.render_batch(jobs)
+    assert "job 1" in str(e.value)
+    films, st = ng.render_batch([])
+    assert films == [] and st["samples"] == 0
