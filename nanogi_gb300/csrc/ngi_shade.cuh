@@ -227,6 +227,39 @@ NGI_D bool bsdf_sample(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0
     return false;
 }
 
+// SampleDirection + EvaluateDirection(forceDegenerated) / EvaluateDirectionPDF in one pass:
+// the sampled direction and the weight fs/pdf the path throughput is multiplied by
+// (src/nanogi.cpp:494-546 / 718-756). False where the reference's fs is zero (path ends).
+// The ratio is formed in closed form where the lobe cancels: R*corr for D, and
+// R*G*F*(wo.H)/(cos_i cos_H)*corr for G (no Beckmann exp); S keeps the explicit ratio.
+template <typename R>
+NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0, R u1, R ucomp, V3<R>& wo,
+                              V3<R>& weight) {
+    if (!bsdf_sample(m, g, wi, u0, u1, ucomp, wo)) return false;
+    if (m.bsdf == BSDF_S) {
+        const V3<R> fs = bsdf_eval(m, g, wi, wo, true);
+        if (is_zero(fs)) return false;
+        weight = fs / bsdf_pdf(m, g, wi, wo);
+        return true;
+    }
+    const V3<R> lwi = to_local(g, wi), lwo = to_local(g, wo);
+    if (lwi.z <= R(0) || lwo.z <= R(0)) return false;
+    const R wiNg = dot(wi, g.gn), woNg = dot(wo, g.gn);
+    if (wiNg * lwi.z <= R(0) || woNg * lwo.z <= R(0)) return false;  // shading-normal correction 0
+    if (m.bsdf == BSDF_D) {
+        if (is_zero(m.R_)) return false;
+        weight = m.R_;
+        return true;
+    }
+    // BSDF_G
+    const V3<R> H = normalize(lwi + lwo);
+    if (H.z <= R(0) || beckmann_d(m.roughness, H) == R(0)) return false;
+    const R G = shadow_masking(lwi, lwo, H);
+    const V3<R> F = fr_conductor(m, dot(lwi, H));
+    weight = m.R_ * (G * dot(lwo, H) / (lwi.z * H.z)) * F;
+    return !is_zero(weight);
+}
+
 // ---- pinhole sensor (rt.hpp:733-739, 955-977, 1189-1211, 1348-1378) -----------------------
 template <typename R>
 NGI_D V3<R> pinhole_direction(const DevSensor<R>& c, R rx, R ry) {

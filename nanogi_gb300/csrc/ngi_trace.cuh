@@ -94,6 +94,13 @@ NGI_D float byte_to_float(uint32_t word, int b) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)) - 8388608.0f;
 }
 
+// 2^23 + byte b of a 32-bit word, as a float (exact): the folded-offset form of byte_to_float.
+NGI_D float byte_bits(uint32_t word, int b) { return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)); }
+
+#ifndef NGI_FOLDED_BOX
+#define NGI_FOLDED_BOX 1
+#endif
+
 // Per-ray state of one CWBVH traversal, kept in registers between steps so a warp can
 // interleave the rays of its lanes (and refill lanes whose ray has finished).
 struct TravState {
@@ -147,6 +154,14 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
     const float ay = (n0.y - s.rp.oy) * s.idy;
     const float az = (n0.z - s.rp.oz) * s.idz;
     const bool nx = s.dneg & 1u, ny = s.dneg & 2u, nz = s.dneg & 4u;
+#if NGI_FOLDED_BOX
+    // Plane distance of quantised coordinate q: q*s + a. The byte permute yields F = 2^23 + q,
+    // so t = F*s + (a - 2^23 s). The folded addend costs up to one quantum |s| of rounding;
+    // moving near planes 2|s| closer and far planes 2|s| farther keeps every box conservative.
+    const float cx = fmaf(-8388608.0f, sx, ax), cy = fmaf(-8388608.0f, sy, ay), cz = fmaf(-8388608.0f, sz, az);
+    const float mx = 2.0f * fabsf(sx), my = 2.0f * fabsf(sy), mz = 2.0f * fabsf(sz);
+    const float anx = cx - mx, afx = cx + mx, any_ = cy - my, afy = cy + my, anz = cz - mz, afz = cz + mz;
+#endif
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
@@ -164,9 +179,15 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
+#if NGI_FOLDED_BOX
+            const float x0 = fmaf(byte_bits(nearx, j), sx, anx), x1 = fmaf(byte_bits(farx, j), sx, afx);
+            const float y0 = fmaf(byte_bits(neary, j), sy, any_), y1 = fmaf(byte_bits(fary, j), sy, afy);
+            const float z0 = fmaf(byte_bits(nearz, j), sz, anz), z1 = fmaf(byte_bits(farz, j), sz, afz);
+#else
             const float x0 = fmaf(byte_to_float(nearx, j), sx, ax), x1 = fmaf(byte_to_float(farx, j), sx, ax);
             const float y0 = fmaf(byte_to_float(neary, j), sy, ay), y1 = fmaf(byte_to_float(fary, j), sy, ay);
             const float z0 = fmaf(byte_to_float(nearz, j), sz, az), z1 = fmaf(byte_to_float(farz, j), sz, az);
+#endif
             const float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
             const float tf = fminf(fminf(x1, y1), fminf(z1, s.tmax));
             if (m != 0u && tn * kBoxLo <= tf * kBoxHi) {

@@ -413,12 +413,10 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                             sa_vprim = prim;
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
-                        V3<R> wo;
-                        if (bsdf_sample(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo)) {
-                            const R pdf = bsdf_pdf(mat, g, wi, wo);
-                            const V3<R> fs = bsdf_eval(mat, g, wi, wo, true);
-                            if (!is_zero(fs)) {
-                                thr = thr * fs / pdf;
+                        V3<R> wo, wgt;
+                        if (bsdf_sample_weight(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo, wgt)) {
+                            {
+                                thr = thr * wgt;
                                 if (ADJ) {
                                     if (nv - 2 >= kAdjMaxPrefix) {
                                         atomicOr(&w.ctr->error_flags, 2);

@@ -1,9 +1,12 @@
 """Batched renders (ngi_render_batch): many independent jobs through one persistent wave.
 
-Every job of a batch must produce the film it produces when rendered alone with the same
-parameters (same Philox paths; only the FP64 summation order differs), whatever the mix of
-scenes, renderers, resolutions, sample counts and path lengths, with and without the
-autotuner.
+Every job of a batch traces the Philox paths it traces when rendered alone with the same
+parameters, whatever the mix of scenes, renderers, resolutions, sample counts and path
+lengths, with and without the autotuner:
+* plain FP64 path: the films are equal up to the FP64 summation order (1e-9);
+* tuned FP32 path: the batch and single-job kernels are separate compilations, so FP32
+  rounding can differ in the last bit and send a few grazing paths elsewhere; the films
+  agree to that level (rel-RMSE 1e-4).
 """
 from __future__ import annotations
 
@@ -28,7 +31,7 @@ def batch_scenes(native_lib, tmp_path_factory):
     cornell.close()
 
 
-def _jobs(batch_scenes, scale=1):
+def _jobs(batch_scenes, scale=1, precision="fp32"):
     import nanogi_gb300 as ng
 
     scenes, jobs, cornell = batch_scenes
@@ -37,33 +40,42 @@ def _jobs(batch_scenes, scale=1):
         res = max(8, j["res"] // 8)
         spp = max(1, j["spp"] // 16) * scale
         out.append((s, ng.Renderer(renderer="pt" if k % 3 == 0 else "ptdirect", num_samples=res * res * spp + k,
-                                   max_num_vertices=j["max_vertices"], width=res, height=res, seed=j["seed"])))
+                                   max_num_vertices=j["max_vertices"], width=res, height=res, seed=j["seed"],
+                                   precision=precision)))
     # the same scene twice, different resolutions / renderers
     out.append((cornell, ng.Renderer(renderer="pt", num_samples=16 * 12 * 40, max_num_vertices=8, width=16, height=12,
-                                     seed=5)))
+                                     seed=5, precision=precision)))
     out.append((cornell, ng.Renderer(renderer="ptdirect", num_samples=24 * 24 * 8, max_num_vertices=-1, width=24,
-                                     height=24, seed=6)))
+                                     height=24, seed=6, precision=precision)))
     return out
 
 
-@pytest.mark.parametrize("autotune", [False, True])
-def test_batch_equals_individual_renders(batch_scenes, autotune):
+def _same(f, ref, precision):
+    if precision == "fp64":
+        return np.allclose(f, ref, rtol=1e-9, atol=1e-12)
+    denom = max(float((ref ** 2).sum()), 1e-300)
+    return float(((f - ref) ** 2).sum()) / denom < 1e-8  # rel-RMSE < 1e-4
+
+
+@pytest.mark.parametrize("autotune,precision", [(False, "fp64"), (True, "fp64"), (False, "fp32"), (True, "fp32")])
+def test_batch_equals_individual_renders(batch_scenes, autotune, precision):
     import nanogi_gb300 as ng
 
-    jobs = _jobs(batch_scenes)
+    jobs = _jobs(batch_scenes, precision=precision)
     films, st = ng.render_batch(jobs, autotune=autotune, autotune_fraction=0.05)
     assert st["samples"] == sum(r.num_samples for _, r in jobs)
     if autotune:
         assert st["trials"] >= 3
     for (scene, r), f in zip(jobs, films):
         ref = r.render(scene)
-        assert np.allclose(f, ref, rtol=1e-9, atol=1e-12), (r.renderer, r.width, r.num_samples)
+        assert _same(f, ref, precision), (r.renderer, r.width, r.num_samples)
+        assert r.last_stats["camera_rays"] == r.num_samples
 
 
 def test_batch_small_wave_and_options(batch_scenes):
     import nanogi_gb300 as ng
 
-    jobs = _jobs(batch_scenes)[:4]
+    jobs = _jobs(batch_scenes, precision="fp64")[:4]
     films, st = ng.render_batch(jobs, wave_size=512, trace_refill=4, iterations_per_graph=2)
     assert st["wave_size"] == 512 and st["trace_refill"] == 4 and st["iterations_per_graph"] == 2
     for (scene, r), f in zip(jobs, films):
