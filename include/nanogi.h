@@ -85,7 +85,17 @@ typedef struct ngi_render_params {
     int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
     int32_t trace_postpone;    /* triangle tests wait while fewer than (value-1)% of a warp's lanes have
                                   some (1..101, 1 = never wait); 0 = auto */
+    int32_t ray_offset;        /* ngi_ray_offset: how rays leave a surface */
 } ngi_render_params;
+
+/* How a ray leaves a surface point. REFERENCE keeps the reference's absolute tmin = EpsF = 1e-4
+ * scene units (Scene::Intersect rt.hpp:2248, Visible rt.hpp:2260); SCALED moves the origin a
+ * fixed number of float ulps along the geometric normal and uses tmin = 0, which holds at any
+ * scene scale (Waechter and Binder, Ray Tracing Gems 2019, ch. 6). */
+typedef enum ngi_ray_offset {
+    NGI_RAY_OFFSET_REFERENCE = 0,
+    NGI_RAY_OFFSET_SCALED = 1
+} ngi_ray_offset;
 
 /* Measurement flags (results in ngi_render_stats). Both change only how the render is
  * launched or instrumented, never its result. */

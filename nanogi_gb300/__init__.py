@@ -141,6 +141,7 @@ class Renderer:
     flags: int = 0
     trace_refill: int = 0
     trace_postpone: int = 0
+    ray_offset: str = "reference"
     last_stats: dict = field(default_factory=dict, repr=False)
 
     def params(self) -> RenderParams:
@@ -161,6 +162,7 @@ class Renderer:
             flags=int(self.flags),
             trace_refill=int(self.trace_refill),
             trace_postpone=int(self.trace_postpone),
+            ray_offset=capi.RAY_OFFSETS[self.ray_offset],
         )
 
     def render(self, scene: Scene, film: np.ndarray | None = None) -> np.ndarray:

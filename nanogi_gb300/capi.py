@@ -26,6 +26,7 @@ STATUS_NAMES = {
 RENDERERS = {"pt": 0, "ptdirect": 1}
 PRECISIONS = {"fp32": 0, "fp64": 1}
 RASTER_MODES = {"stratified": 0, "uniform": 1}
+RAY_OFFSETS = {"reference": 0, "scaled": 1}
 
 
 class RenderParams(ctypes.Structure):
@@ -44,6 +45,7 @@ class RenderParams(ctypes.Structure):
         ("flags", ctypes.c_int32),
         ("trace_refill", ctypes.c_int32),
         ("trace_postpone", ctypes.c_int32),
+        ("ray_offset", ctypes.c_int32),
     ]
 
 

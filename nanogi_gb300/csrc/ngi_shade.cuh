@@ -14,7 +14,16 @@ struct Geom {
     V3<R> p, sn, gn, du, dv;  // du = dpdu, dv = dpdv: tangent frame (du, dv, sn)
     R uvx, uvy;
     bool degenerated;
+    float ext;  // largest |coordinate| of the triangle under p (scale of its rounding error); 0 off surfaces
 };
+
+// Largest |coordinate| over three points.
+template <typename R>
+NGI_D float max_abs3(V3<R> a, V3<R> b, V3<R> c) {
+    const R m = fmax_(fmax_(fmax_(fabs_(a.x), fabs_(a.y)), fmax_(fabs_(a.z), fabs_(b.x))),
+                      fmax_(fmax_(fabs_(b.y), fabs_(b.z)), fmax_(fmax_(fabs_(c.x), fabs_(c.y)), fabs_(c.z))));
+    return (float)m;
+}
 
 template <typename R> NGI_D R kPi_() { return R(3.14159265358979323846); }
 template <typename R> NGI_D R kInvPi_() { return R(1.0 / 3.14159265358979323846); }
@@ -315,6 +324,7 @@ NGI_D void sample_mesh_position(const SceneView<R>& sv, int tri_base, int tri_co
     g.uvx = (R)T[0] * (R(1) - b0 - b1) + (R)T[2] * b0 + (R)T[4] * b1;
     g.uvy = (R)T[1] * (R(1) - b0 - b1) + (R)T[3] * b0 + (R)T[5] * b1;
     g.degenerated = false;
+    g.ext = max_abs3(p1, p2, p3);
     g.gn = normalize(cross(p2 - p1, p3 - p1));
     g.sn = g.gn;
     tangent_space(g);

@@ -97,8 +97,11 @@ NGI_D float byte_to_float(uint32_t word, int b) {
 // 2^23 + byte b of a 32-bit word, as a float (exact): the folded-offset form of byte_to_float.
 NGI_D float byte_bits(uint32_t word, int b) { return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)); }
 
+// The folded form saves one subtraction per plane but widens every box by two quanta; on the
+// 1.55M-triangle terrain it ran 6% slower (1010 vs 1076 Mrays/s), so the exact form is the
+// default.
 #ifndef NGI_FOLDED_BOX
-#define NGI_FOLDED_BOX 1
+#define NGI_FOLDED_BOX 0
 #endif
 
 // Per-ray state of one CWBVH traversal, kept in registers between steps so a warp can

@@ -72,6 +72,7 @@ struct RenderConsts {
     int trace_refill;       // idle lanes that trigger a traversal warp's refill
     int trace_postpone;     // triangle-postponing threshold (percent of active lanes), -1 = default
     int num_prims;          // primitives of the scene (adjoint gradient layout)
+    int ray_offset;         // NGI_RAY_OFFSET_*: absolute tmin = EpsF, or scale-aware origin offsets
 };
 
 // One job of a batch render: its scene, parameters, device film and first batch sample.
@@ -165,7 +166,7 @@ NGI_D void film_add(double* film, uint32_t pixel, V3<R> c) {
 template <typename R>
 struct ShadowRay {
     bool valid;
-    float ox, oy, oz, dx, dy, dz, tmax;
+    float ox, oy, oz, dx, dy, dz, tmin, tmax;
     V3<R> c;
     uint32_t pixel;
     int light_prim;  // adjoint: primitive whose Le scales the contribution
@@ -258,6 +259,7 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
     } else {
         gl.p = L.position;
         gl.degenerated = true;
+        gl.ext = 0.0f;
         pdf_pos = R(1);
     }
     const V3<R> ppl = normalize(gl.p - g.p);
@@ -294,7 +296,9 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
     const R len = sqrt_(dot(d, d));
     const V3<R> dn = d / len;
     out.valid = true;
-    out.ox = (float)g.p.x; out.oy = (float)g.p.y; out.oz = (float)g.p.z;
+    const float4 ro = ray_origin(g, dn, rc.ray_offset);
+    out.ox = ro.x; out.oy = ro.y; out.oz = ro.z;
+    out.tmin = ro.w;
     out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
     out.tmax = (float)len * (1.0f - kEpsF);
     out.c = C;
@@ -302,12 +306,35 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
     out.light_prim = L.prim;
 }
 
+// Float origin and tmin of a ray leaving surface point g in direction d. REFERENCE: the
+// reference's absolute tmin = EpsF (Scene::Intersect, rt.hpp:2248). SCALED: tmin = 0 and the
+// origin moves off the surface, to d's side of the geometric normal, by 2^-17 of the largest
+// |coordinate| of the surface triangle. The hit point is an affine combination of that
+// triangle's vertices, so its distance from the triangle's plane is a few ulps of that
+// magnitude, and so is the error of any later plane test against it; 2^-17 is 64..128 such
+// ulps. The offset grows with the local geometry, not with the scene, so millimetre
+// triangles near the origin and kilometre walls both keep clear of self-intersection.
+constexpr float kOffsetScale = 1.0f / 131072.0f;
+
 template <typename R>
-NGI_D void store_ray(const WaveView<R>& w, int s, V3<R> o, V3<R> d) {
-    w.ray_o[s] = make_float4((float)o.x, (float)o.y, (float)o.z, kEpsF);
+NGI_D float4 ray_origin(const Geom<R>& g, V3<R> d, int mode) {
+    if (mode != NGI_RAY_OFFSET_SCALED) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, kEpsF);
+    if (g.degenerated || !(g.ext > 0.0f)) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, 0.0f);
+    const R delta = (R)(g.ext * kOffsetScale);
+    const V3<R> o = g.p + g.gn * (dot(g.gn, d) >= R(0) ? delta : -delta);
+    return make_float4((float)o.x, (float)o.y, (float)o.z, 0.0f);
+}
+
+template <typename R>
+NGI_D void store_ray(const WaveView<R>& w, int s, const Geom<R>& g, V3<R> d, int mode) {
+    const V3<R> o = g.p;
+    const float4 ro = ray_origin(g, d, mode);
+    w.ray_o[s] = ro;
     w.ray_d[s] = make_float4((float)d.x, (float)d.y, (float)d.z, kInfF);
     if (sizeof(R) == 8) {
-        w.od_o[s] = Vec4T<double>{(double)o.x, (double)o.y, (double)o.z, 0.0};
+        // the hit point is reconstructed from the origin the ray was traced from
+        if (mode == NGI_RAY_OFFSET_SCALED) w.od_o[s] = Vec4T<double>{(double)ro.x, (double)ro.y, (double)ro.z, 0.0};
+        else w.od_o[s] = Vec4T<double>{(double)o.x, (double)o.y, (double)o.z, 0.0};
         w.od_d[s] = Vec4T<double>{(double)d.x, (double)d.y, (double)d.z, 0.0};
     }
 }
@@ -363,7 +390,6 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
 
                 // Hit reconstruction (Scene::Intersect rt.hpp:2196-2233)
                 Geom<R> g;
-                g.p = o + d * (R)h.x;
                 const float4* tp = sv.tris + 3 * (size_t)ti;
                 const float4 q1 = tp[0], q2 = tp[1], q3 = tp[2];
                 const V3<R> p1 = v3<R>(q1.x, q1.y, q1.z), p2 = v3<R>(q2.x, q2.y, q2.z), p3 = v3<R>(q3.x, q3.y, q3.z);
@@ -371,6 +397,14 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                 const float4* np = sv.nrm + 3 * (size_t)ti;
                 const float4 m1 = np[0], m2 = np[1], m3 = np[2];
                 const float bw = 1.0f - h.y - h.z;
+                if (rc.ray_offset == NGI_RAY_OFFSET_SCALED) {
+                    // on the triangle itself, whatever the distance travelled
+                    g.p = p1 * (R)bw + p2 * (R)h.y + p3 * (R)h.z;
+                    g.ext = max_abs3(p1, p2, p3);
+                } else {
+                    g.p = o + d * (R)h.x;
+                    g.ext = 0.0f;
+                }
                 g.sn = normalize(v3<R>(m1.x, m1.y, m1.z) * (R)bw + v3<R>(m2.x, m2.y, m2.z) * (R)h.y +
                                  v3<R>(m3.x, m3.y, m3.z) * (R)h.z);
                 if (isnan_(g.sn.x) || isnan_(g.sn.y) || isnan_(g.sn.z)) g.sn = g.gn;
@@ -426,7 +460,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                                         w.pre[2 * (size_t)s + 1] = pb;
                                     }
                                 }
-                                store_ray(w, s, g.p, wo);
+                                store_ray(w, s, g, wo, rc.ray_offset);
                                 w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
                                 w.nverts[s] = nv;
                                 alive = true;
@@ -443,7 +477,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
         {
             const int q = warp_append(&w.ctr->sh_count, sa.valid);
             if (sa.valid) {
-                w.sh_o[q] = make_float4(sa.ox, sa.oy, sa.oz, kEpsF);
+                w.sh_o[q] = make_float4(sa.ox, sa.oy, sa.oz, sa.tmin);
                 w.sh_d[q] = make_float4(sa.dx, sa.dy, sa.dz, sa.tmax);
                 w.sh_c[q] = Vec4T<R>{sa.c.x, sa.c.y, sa.c.z, R(0)};
                 w.sh_pix[q] = sa.pixel;
@@ -503,6 +537,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                     if (cam.type == ET_PINHOLE) {
                         ge.p = cam.eye;
                         ge.degenerated = true;
+                        ge.ext = 0.0f;
                         ge.sn = ge.gn = ge.du = ge.dv = v3<R>(0, 0, 0);
                         ge.uvx = ge.uvy = R(0);
                         thr = v3<R>(1, 1, 1);
@@ -549,7 +584,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                         else thr = thr * cam.We / kInvPi_<R>();
                     }
                     if (ok) {
-                        store_ray(w, s, ge.p, wo);
+                        store_ray(w, s, ge, wo, rc.ray_offset);
                         w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
                         w.pixel[s] = pix;
                         w.sample[s] = gsample;
@@ -570,7 +605,7 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
         {
             const int q = warp_append(&w.ctr->sh_count, sb.valid);
             if (sb.valid) {
-                w.sh_o[q] = make_float4(sb.ox, sb.oy, sb.oz, kEpsF);
+                w.sh_o[q] = make_float4(sb.ox, sb.oy, sb.oz, sb.tmin);
                 w.sh_d[q] = make_float4(sb.dx, sb.dy, sb.dz, sb.tmax);
                 w.sh_c[q] = Vec4T<R>{sb.c.x, sb.c.y, sb.c.z, R(0)};
                 w.sh_pix[q] = sb.pixel;
@@ -1161,6 +1196,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.ray_offset = p.ray_offset;
     rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
@@ -1382,6 +1418,7 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
         const long long wh = (long long)p.width * p.height;
         rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
         rc.trace_refill = p.trace_refill;
+    rc.ray_offset = p.ray_offset;
     rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
         const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
@@ -1441,8 +1478,10 @@ RenderConsts consts_of(const ngi_render_params& p, int num_prims) {
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.ray_offset = p.ray_offset;
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     rc.num_prims = num_prims;
+    rc.ray_offset = p.ray_offset;
     return rc;
 }
 
@@ -1769,6 +1808,7 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
     const long long wh = (long long)p.width * p.height;
     rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
     rc.trace_refill = p.trace_refill;
+    rc.ray_offset = p.ray_offset;
     rc.num_prims = (int)hs.prims.size();
     rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;

@@ -15,6 +15,7 @@ Workloads (sizes from the benchmark configurations):
 """
 from __future__ import annotations
 
+import copy
 import math
 import os
 from dataclasses import dataclass, field
@@ -171,6 +172,21 @@ def pinhole(eye, center, up, fov) -> Primitive:
 def phong_to_beckmann(n: float) -> float:
     """Beckmann roughness matching a Phong lobe exponent (Walter et al. 2007): sqrt(2/(n+2))."""
     return math.sqrt(2.0 / (n + 2.0))
+
+
+def transformed(desc: SceneDesc, scale: float, offset=(0.0, 0.0, 0.0)) -> SceneDesc:
+    """The scene scaled by `scale` about the origin and moved by `offset`: mesh positions and
+    pinhole eye/center. Radiance is unchanged, so every image of the scene is unchanged."""
+    d = copy.deepcopy(desc)
+    off = np.asarray(offset, np.float64)
+    for p in d.primitives:
+        if p.mesh is not None:
+            p.mesh.positions = _f32(p.mesh.positions.astype(np.float64) * scale + off)
+        if "E" in p.type and p.params["E"]["type"] == "pinhole":
+            v = p.params["E"]["pinhole"]["view"]
+            v["eye"] = [float(x) for x in np.asarray(v["eye"], np.float64) * scale + off]
+            v["center"] = [float(x) for x in np.asarray(v["center"], np.float64) * scale + off]
+    return d
 
 
 # ---- workloads -------------------------------------------------------------------------------------

@@ -63,6 +63,7 @@ struct Geom {
     bool degenerated = false;
     dv3 p, sn, gn, dpdu, dpdv;
     double uv[2] = {0, 0};
+    float ext = 0.0f;  // largest |coordinate| of the triangle under p (scaled ray offsets only)
     void ComputeTangentSpace() {
         // OrthonormalBasis(sn, dpdu, dpdv) (rt.hpp:55-59)
         const dv3 a = sn;
@@ -411,8 +412,16 @@ struct Isect {
     int prim = -1;
 };
 
-// Scene::Intersect (rt.hpp:2162-2244)
-bool Intersect(const ora_scene& s, bool use_bvh, dv3 o, dv3 d, Isect& is, float minT, float maxT) {
+float MaxAbs3(dv3 a, dv3 b, dv3 c) {
+    double m = 0.0;
+    for (double x : {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z}) m = std::max(m, std::fabs(x));
+    return (float)m;
+}
+
+// Scene::Intersect (rt.hpp:2162-2244); offset_mode 1 puts the hit point on the triangle
+// (barycentric) instead of at o + t d, for the scaled ray offsets.
+bool Intersect(const ora_scene& s, bool use_bvh, dv3 o, dv3 d, Isect& is, float minT, float maxT,
+               int offset_mode = 0) {
     const float of[3] = {(float)o.x, (float)o.y, (float)o.z};
     const float df[3] = {(float)d.x, (float)d.y, (float)d.z};
     const RayF r = MakeRay(of, df);
@@ -420,13 +429,19 @@ bool Intersect(const ora_scene& s, bool use_bvh, dv3 o, dv3 d, Isect& is, float 
     if (h.tri < 0) return false;
     const int f = h.tri;
     is.prim = s.tri_prim[f];
-    is.geom.p = o + d * (double)h.t;
     const double* P = &s.pos[9 * (size_t)f];
     const dv3 p1(P[0], P[1], P[2]), p2(P[3], P[4], P[5]), p3(P[6], P[7], P[8]);
     is.geom.gn = normalize(cross(p2 - p1, p3 - p1));
     const double* N = &s.nrm[9 * (size_t)f];
     const dv3 n1(N[0], N[1], N[2]), n2(N[3], N[4], N[5]), n3(N[6], N[7], N[8]);
     const float w = 1.0f - h.u - h.v;
+    if (offset_mode == 1) {
+        is.geom.p = p1 * (double)w + p2 * (double)h.u + p3 * (double)h.v;
+        is.geom.ext = MaxAbs3(p1, p2, p3);
+    } else {
+        is.geom.p = o + d * (double)h.t;
+        is.geom.ext = 0.0f;
+    }
     is.geom.sn = normalize(n1 * (double)w + n2 * (double)h.u + n3 * (double)h.v);
     if (std::isnan(is.geom.sn.x) || std::isnan(is.geom.sn.y) || std::isnan(is.geom.sn.z)) is.geom.sn = is.geom.gn;
     const double* T = &s.uv[6 * (size_t)f];
@@ -437,16 +452,38 @@ bool Intersect(const ora_scene& s, bool use_bvh, dv3 o, dv3 d, Isect& is, float 
     return true;
 }
 
-bool Visible(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2) {
-    const dv3 v = p2 - p1;
-    const double len = length(v);
-    const dv3 d = v / len;
+// Ray origin (a float point, held in doubles) and tmin for a ray leaving g toward d.
+// Mode 0 is the reference's absolute tmin = EpsF (rt.hpp:2248). Mode 1 (not in the
+// reference) uses tmin = 0 and moves the origin 2^-17 x (largest |coordinate| of the
+// surface triangle) along the geometric normal, to d's side.
+dv3 RayOrigin(const Geom& g, dv3 d, int mode, float& tmin) {
+    if (mode != 1) {
+        tmin = EpsF;
+        return g.p;
+    }
+    tmin = 0.0f;
+    dv3 o = g.p;
+    if (!g.degenerated && g.ext > 0.0f) {
+        const double delta = (double)(g.ext * (1.0f / 131072.0f));
+        o = g.p + g.gn * (dot(g.gn, d) >= 0.0 ? delta : -delta);
+    }
+    return dv3((float)o.x, (float)o.y, (float)o.z);
+}
+
+// Scene::Visible (rt.hpp:2254-2262) from origin p1 with minimum distance tmin
+bool VisibleFrom(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2, dv3 d, float tmin) {
+    const double len = length(p2 - p1);
     const float of[3] = {(float)p1.x, (float)p1.y, (float)p1.z};
     const float df[3] = {(float)d.x, (float)d.y, (float)d.z};
     const RayF r = MakeRay(of, df);
     const float tmax = (float)len * (1.0f - EpsF);
-    const Hit h = use_bvh ? IntersectBvh(s, r, EpsF, tmax, true) : IntersectBrute(s, r, EpsF, tmax, true);
+    const Hit h = use_bvh ? IntersectBvh(s, r, tmin, tmax, true) : IntersectBrute(s, r, tmin, tmax, true);
     return h.tri < 0;
+}
+
+bool Visible(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2) {
+    const dv3 v = p2 - p1;
+    return VisibleFrom(s, use_bvh, p1, p2, v / length(v), EpsF);
 }
 
 // ---- Primitive methods (rt.hpp:483-1466) ------------------------------------------------------
@@ -514,6 +551,7 @@ void SampleTriangleMesh(const ora_scene& s, const Prim& p, double u0, double u1,
     g.uv[0] = T[0] * (1.0 - b0 - b1) + T[2] * b0 + T[4] * b1;
     g.uv[1] = T[1] * (1.0 - b0 - b1) + T[3] * b0 + T[5] * b1;
     g.degenerated = false;
+    g.ext = MaxAbs3(p1, p2, p3);
     g.gn = normalize(cross(p2 - p1, p3 - p1));
     g.sn = g.gn;
     g.ComputeTangentSpace();
@@ -816,7 +854,9 @@ void ProcessSample(RenderCtx& c, Sampler& smp) {
             // Only trace the shadow ray when it can matter (same result as always tracing)
             if (!is_zero(Cpre * fsL)) {
                 c.sh++;
-                Vis = Visible(s, bvh, geom.p, geomL.p) ? 1.0 : 0.0;
+                float tmin;
+                const dv3 o = RayOrigin(geom, ppL, P.ray_offset, tmin);
+                Vis = VisibleFrom(s, bvh, o, geomL.p, ppL, tmin) ? 1.0 : 0.0;
             }
             const dv3 C = throughput * fsE * Gt * Vis * fsL * 1.0 / pdfL / pdfPL;
             if (!is_zero(C)) {
@@ -849,7 +889,9 @@ void ProcessSample(RenderCtx& c, Sampler& smp) {
         throughput = throughput * fs / pdfD;
         Isect is;
         c.ext++;
-        if (!Intersect(s, bvh, geom.p, wo, is, EpsF, InfF)) break;
+        float tmin;
+        const dv3 ro = RayOrigin(geom, wo, P.ray_offset, tmin);
+        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) break;
         const Prim& hp = s.prims[is.prim];
         if (!direct && (hp.d.type & L)) {
             const dv3 Le = EvaluateDirection(hp, is.geom, L, dv3(), -wo, false, false);

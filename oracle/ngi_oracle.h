@@ -55,6 +55,8 @@ typedef struct ora_render_params {
     int32_t num_threads;    /* 0 = all hardware threads */
     int32_t use_bvh;        /* 1: own BVH (fast), 0: brute force (truth) */
     int64_t grain_size;     /* samples per work item (TBB grain size, src/nanogi.cpp:2014) */
+    int32_t ray_offset;     /* 0: absolute tmin = EpsF (rt.hpp:2248); 1: scale-aware origin offset, tmin 0 */
+    int32_t pad_;
 } ora_render_params;
 
 typedef struct ora_render_stats {

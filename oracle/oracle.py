@@ -54,6 +54,7 @@ class RenderParams(ctypes.Structure):
         ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("seed", ctypes.c_uint64),
         ("sample_offset", ctypes.c_int64), ("rng_mode", ctypes.c_int32), ("raster_mode", ctypes.c_int32),
         ("num_threads", ctypes.c_int32), ("use_bvh", ctypes.c_int32), ("grain_size", ctypes.c_int64),
+        ("ray_offset", ctypes.c_int32), ("pad_", ctypes.c_int32),
     ]
 
 
@@ -216,12 +217,14 @@ class OracleScene:
         return out.astype(bool)
 
     def render(self, renderer="pt", num_samples=1000, max_vertices=-1, width=16, height=16, seed=0,
-               sample_offset=0, rng_mode="replay", raster="stratified", threads=0, use_bvh=True, grain=1000):
+               sample_offset=0, rng_mode="replay", raster="stratified", threads=0, use_bvh=True, grain=1000,
+               ray_offset="reference"):
         p = RenderParams(renderer={"pt": 0, "ptdirect": 1}[renderer], max_vertices=max_vertices,
                          num_samples=num_samples, width=width, height=height, seed=seed & 0xFFFFFFFFFFFFFFFF,
                          sample_offset=sample_offset, rng_mode={"reference": 0, "replay": 1}[rng_mode],
                          raster_mode={"stratified": 0, "uniform": 1}[raster], num_threads=threads,
-                         use_bvh=int(use_bvh), grain_size=grain)
+                         use_bvh=int(use_bvh), grain_size=grain,
+                         ray_offset={"reference": 0, "scaled": 1}[ray_offset])
         film = np.zeros((height, width, 3), np.float64)
         st = RenderStats()
         if lib().ora_render(self._h, ctypes.byref(p), _p(film), ctypes.byref(st)) != 0:

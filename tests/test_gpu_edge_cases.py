@@ -201,3 +201,27 @@ def test_gpu_matches_committed_golden_films(native_lib, tmp_path):
         ref = np.load(golden / case["file"])
         assert rel_rmse(f, ref) < 1e-4, case["file"]
         scene.close()
+
+
+@pytest.mark.parametrize("scale", [1e-3, 1.0, 1e3])
+def test_scaled_ray_offsets_replay_the_oracle(native_lib, tmp_path, scale):
+    """ray_offset="scaled": the FP64 path replays the oracle's scaled-offset render of the Cornell
+    box at 1e-3, 1 and 1e3 scene units, and the FP32 path gives the same image at every scale."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    W = H = 16
+    n = W * H * 32
+    desc = scenegen.transformed(scenegen.cornell_box(), scale)
+    scene = _scene(scenegen.write_scene(desc, tmp_path), 1.0)
+    f64 = _r(renderer="ptdirect", num_samples=n, max_num_vertices=8, width=W, height=H, seed=12, precision="fp64",
+             ray_offset="scaled").render(scene)
+    ref = OracleScene.from_desc(desc, 1.0).render("ptdirect", num_samples=n, max_vertices=8, width=W, height=H,
+                                                  seed=12, rng_mode="replay", use_bvh=False, ray_offset="scaled")
+    assert rel_rmse(f64, ref) < 1e-6
+    unit = OracleScene.from_desc(scenegen.cornell_box(), 1.0).render(
+        "ptdirect", num_samples=n, max_vertices=8, width=W, height=H, seed=12, rng_mode="replay", use_bvh=False,
+        ray_offset="scaled")
+    f32 = _r(renderer="ptdirect", num_samples=n, max_num_vertices=8, width=W, height=H, seed=12,
+             ray_offset="scaled").render(scene)
+    assert rel_rmse(f32, unit) < 1e-3

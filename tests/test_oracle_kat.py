@@ -175,3 +175,25 @@ def test_golden_films(oracle_lib):
                         use_bvh=False, threads=1)
         ref = np.load(GOLDEN / case["file"])
         assert np.allclose(film, ref, rtol=1e-12, atol=1e-15), case["file"]
+
+
+def test_scaled_ray_offsets_are_scale_invariant(oracle_lib):
+    """The Cornell box scaled by 1e-3 and 1e3 renders the same image (same Philox paths) with
+    scaled ray offsets, while the reference's absolute tmin = 1e-4 (rt.hpp:2248) skips real
+    contacts at 1e-3 and self-intersects at 1e3."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    base = scenegen.cornell_box()
+    kw = dict(num_samples=24 * 24 * 32, max_vertices=8, width=24, height=24, seed=3, use_bvh=True)
+    unit = OracleScene.from_desc(base, 1.0).render("ptdirect", ray_offset="scaled", **kw)
+
+    def rel(a, b):
+        return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+    for scale in (1e-3, 1e3):
+        d = scenegen.transformed(base, scale)
+        f = OracleScene.from_desc(d, 1.0).render("ptdirect", ray_offset="scaled", **kw)
+        assert rel(f, unit) < 1e-4, scale
+    big = OracleScene.from_desc(scenegen.transformed(base, 1e3), 1.0).render("ptdirect", **kw)
+    assert big.sum() < 0.95 * unit.sum()  # shadow rays that hit their own surface
