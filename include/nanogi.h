@@ -149,6 +149,25 @@ NGI_API int32_t ngi_abi_version(void);
  * flattens them into host SoA arrays. Does not touch the GPU. */
 NGI_API ngi_status ngi_scene_load(const char* yaml_path, double aspect, ngi_scene** out_scene);
 
+/* A triangle mesh held by the caller (Mesh::Positions / Normals / Texcoords / Faces,
+ * rt.hpp:148-155). It stands in for the mesh file that a primitive's `mesh: path:` names. */
+typedef struct ngi_mesh_data {
+    const char* path;            /* matched verbatim against the scene file's mesh paths */
+    const float* positions;      /* 3 per vertex */
+    const float* normals;        /* 3 per vertex, or NULL for flat face normals */
+    const float* texcoords;      /* 2 per vertex, or NULL */
+    const uint32_t* faces;       /* 3 vertex indices per triangle, 0-based */
+    int64_t num_vertices;
+    int64_t num_triangles;
+} ngi_mesh_data;
+
+/* ngi_scene_load, with meshes taken from memory: a primitive whose mesh path equals the path
+ * of one of `meshes` reads that mesh instead of the file (other paths still load from disk).
+ * The arrays are copied; the caller may free them on return. No reference counterpart: the
+ * reference reads every mesh through Assimp (rt.hpp:1640-1730). */
+NGI_API ngi_status ngi_scene_load_with_meshes(const char* yaml_path, double aspect, const ngi_mesh_data* meshes,
+                                              int32_t num_meshes, ngi_scene** out_scene);
+
 /* Scene::~Scene  include/nanogi/rt.hpp:1509-1513. Frees host and device memory. */
 NGI_API void ngi_scene_free(ngi_scene* scene);
 

@@ -41,6 +41,30 @@ class Scene:
         check(lib.ngi_scene_load(os.fsencode(str(path)), float(aspect), ctypes.byref(h)))
         return cls(h.value)
 
+    @classmethod
+    def load_with_meshes(cls, path: str | os.PathLike, aspect: float, meshes: dict) -> "Scene":
+        """Like ``load``, but a mesh path that is a key of ``meshes`` takes that mesh from memory:
+        ``{path: (positions (V,3) float32, faces (F,3) uint32[, normals (V,3) float32 or None[, uvs (V,2)
+        float32 or None]])}``."""
+        lib = load_library()
+        keep = []
+        arr = (capi.MeshData * max(len(meshes), 1))()
+
+        def opt(m, k, cols):
+            return None if len(m) <= k or m[k] is None else np.ascontiguousarray(m[k], np.float32).reshape(-1, cols)
+
+        for i, (name, m) in enumerate(meshes.items()):
+            pos = np.ascontiguousarray(m[0], np.float32).reshape(-1, 3)
+            faces = np.ascontiguousarray(m[1], np.uint32).reshape(-1, 3)
+            nrm, uv = opt(m, 2, 3), opt(m, 3, 2)
+            keep += [pos, faces, nrm, uv]
+            arr[i] = capi.MeshData(os.fsencode(str(name)), pos.ctypes.data, None if nrm is None else nrm.ctypes.data,
+                                   None if uv is None else uv.ctypes.data, faces.ctypes.data, pos.shape[0],
+                                   faces.shape[0])
+        h = ctypes.c_void_p()
+        check(lib.ngi_scene_load_with_meshes(os.fsencode(str(path)), float(aspect), arr, len(meshes), ctypes.byref(h)))
+        return cls(h.value)
+
     @property
     def handle(self) -> ctypes.c_void_p:
         if not self._h:

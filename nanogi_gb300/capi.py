@@ -117,12 +117,26 @@ class BatchStats(ctypes.Structure):
     ]
 
 
+class MeshData(ctypes.Structure):
+    _fields_ = [
+        ("path", ctypes.c_char_p),
+        ("positions", ctypes.c_void_p),
+        ("normals", ctypes.c_void_p),
+        ("texcoords", ctypes.c_void_p),
+        ("faces", ctypes.c_void_p),
+        ("num_vertices", ctypes.c_int64),
+        ("num_triangles", ctypes.c_int64),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/nanogi.h declares
 _P = ctypes.POINTER
 PROTOTYPES = {
     "ngi_last_error": (ctypes.c_char_p, []),
     "ngi_abi_version": (ctypes.c_int32, []),
     "ngi_scene_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, _P(ctypes.c_void_p)]),
+    "ngi_scene_load_with_meshes": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, _P(MeshData), ctypes.c_int32,
+                                                  _P(ctypes.c_void_p)]),
     "ngi_scene_free": (None, [ctypes.c_void_p]),
     "ngi_scene_get_info": (ctypes.c_int, [ctypes.c_void_p, _P(SceneInfo)]),
     "ngi_scene_get_triangles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

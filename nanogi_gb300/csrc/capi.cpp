@@ -99,6 +99,44 @@ NGI_API ngi_status ngi_scene_load(const char* yaml_path, double aspect, ngi_scen
     });
 }
 
+NGI_API ngi_status ngi_scene_load_with_meshes(const char* yaml_path, double aspect, const ngi_mesh_data* meshes,
+                                              int32_t num_meshes, ngi_scene** out_scene) {
+    if (!out_scene) return Fail(NGI_ERR_INVALID_ARGUMENT, "out_scene is NULL");
+    *out_scene = nullptr;
+    if (!yaml_path) return Fail(NGI_ERR_INVALID_ARGUMENT, "path is NULL");
+    if (num_meshes < 0 || (num_meshes > 0 && !meshes))
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "meshes is NULL or num_meshes is negative");
+    std::vector<ngi::MemoryMesh> held((size_t)num_meshes);
+    for (int32_t i = 0; i < num_meshes; i++) {
+        const ngi_mesh_data& m = meshes[i];
+        const std::string which = "mesh " + std::to_string(i);
+        if (!m.path) return Fail(NGI_ERR_INVALID_ARGUMENT, which + ": path is NULL");
+        if (m.num_vertices < 0 || m.num_triangles < 0)
+            return Fail(NGI_ERR_INVALID_ARGUMENT, which + ": negative vertex or triangle count");
+        if (m.num_triangles > 0 && (!m.positions || !m.faces))
+            return Fail(NGI_ERR_INVALID_ARGUMENT, which + ": positions or faces is NULL");
+        if (m.num_vertices > 0xFFFFFFFFll || m.num_triangles > 0x7FFFFFFFll)
+            return Fail(NGI_ERR_INVALID_ARGUMENT, which + ": too many vertices or triangles");
+        for (int64_t k = 0; k < 3 * m.num_triangles; k++)
+            if ((int64_t)m.faces[k] >= m.num_vertices)
+                return Fail(NGI_ERR_INVALID_ARGUMENT, which + ": face index out of range");
+        held[i].path = m.path;
+        held[i].positions = m.positions;
+        held[i].normals = m.normals;
+        held[i].texcoords = m.texcoords;
+        held[i].faces = m.faces;
+        held[i].num_vertices = m.num_vertices;
+        held[i].num_triangles = m.num_triangles;
+    }
+    return Guard([&]() {
+        auto host = ngi::LoadScene(yaml_path, aspect, &held);
+        auto* s = new ngi_scene();
+        s->host = std::move(host);
+        *out_scene = s;
+        return NGI_OK;
+    });
+}
+
 NGI_API void ngi_scene_free(ngi_scene* scene) {
     if (!scene) return;
     try {

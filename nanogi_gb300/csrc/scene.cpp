@@ -66,7 +66,55 @@ void CreateTriangleAreaDist(const HostScene& s, HostPrimitive& prim) {
 
 }  // namespace
 
-std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect) {
+namespace {
+
+// Appends a caller-held mesh to the flattened triangle arrays; returns its vertex count.
+int64_t AppendMemoryMesh(HostScene& scene, HostPrimitive& prim, const MemoryMesh& m, double* bmin, double* bmax) {
+    prim.has_mesh = true;
+    prim.has_uv = m.texcoords != nullptr;
+    prim.tri_first = scene.NumTriangles();
+    prim.tri_count = m.num_triangles;
+    const size_t nt = (size_t)m.num_triangles;
+    const size_t base = scene.tri_pos.size() / 9;
+    scene.tri_pos.resize(9 * (base + nt));
+    scene.tri_nrm.resize(9 * (base + nt));
+    scene.tri_uv.resize(6 * (base + nt), 0.0f);
+    scene.tri_prim.resize(base + nt, (int32_t)scene.prims.size());
+    for (int64_t v = 0; v < m.num_vertices; v++)
+        for (int k = 0; k < 3; k++) {
+            bmin[k] = std::fmin(bmin[k], (double)m.positions[3 * v + k]);
+            bmax[k] = std::fmax(bmax[k], (double)m.positions[3 * v + k]);
+        }
+    float* P = scene.tri_pos.data() + 9 * base;
+    float* N = scene.tri_nrm.data() + 9 * base;
+    float* T = scene.tri_uv.data() + 6 * base;
+    for (size_t f = 0; f < nt; f++) {
+        const uint32_t* ix = m.faces + 3 * f;
+        for (int c = 0; c < 3; c++) {
+            for (int k = 0; k < 3; k++) P[9 * f + 3 * c + k] = m.positions[3 * (size_t)ix[c] + k];
+            if (m.normals)
+                for (int k = 0; k < 3; k++) N[9 * f + 3 * c + k] = m.normals[3 * (size_t)ix[c] + k];
+            if (m.texcoords)
+                for (int k = 0; k < 2; k++) T[6 * f + 2 * c + k] = m.texcoords[2 * (size_t)ix[c] + k];
+        }
+        if (!m.normals) {
+            // flat normals (aiProcess_GenNormals, rt.hpp:1655-1663)
+            const float* q = P + 9 * f;
+            const double e1[3] = {(double)q[3] - q[0], (double)q[4] - q[1], (double)q[5] - q[2]};
+            const double e2[3] = {(double)q[6] - q[0], (double)q[7] - q[1], (double)q[8] - q[2]};
+            double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int k = 0; k < 3; k++) n[k] = l > 0 ? n[k] / l : 0.0;
+            for (int c = 0; c < 3; c++)
+                for (int k = 0; k < 3; k++) N[9 * f + 3 * c + k] = (float)n[k];
+        }
+    }
+    return m.num_vertices;
+}
+
+}  // namespace
+
+std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect, const std::vector<MemoryMesh>* memory) {
     if (!(aspect > 0) || !std::isfinite(aspect)) throw SceneError(kErrArg, "aspect must be positive and finite");
     {
         std::ifstream probe(path);
@@ -125,36 +173,44 @@ std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect) {
                     const YamlNode& pp = mn["postprocess"];
                     smooth = pp.Has("generate_smooth_normals") && pp["generate_smooth_normals"].AsBool();
                 }
-                ObjMesh mesh;
-                try {
-                    mesh = LoadObj(base + local, smooth);
-                } catch (const std::ios_base::failure& e) {
-                    throw SceneError(kErrIO, e.what());
-                } catch (const ObjError& e) {
-                    throw SceneError(kErrParse, e.what());
-                }
-                prim.has_mesh = true;
-                prim.has_uv = !mesh.texcoords.empty();
-                prim.tri_first = scene->NumTriangles();
-                prim.tri_count = (int64_t)(mesh.faces.size() / 3);
-                const size_t nv = mesh.positions.size() / 3;
-                for (size_t v = 0; v < nv; v++)
-                    for (int k = 0; k < 3; k++) {
-                        bmin[k] = std::fmin(bmin[k], mesh.positions[3 * v + k]);
-                        bmax[k] = std::fmax(bmax[k], mesh.positions[3 * v + k]);
+                const MemoryMesh* held = nullptr;
+                if (memory)
+                    for (const MemoryMesh& m : *memory)
+                        if (m.path == local) held = &m;
+                if (held) {
+                    scene->num_vertices += AppendMemoryMesh(*scene, prim, *held, bmin, bmax);
+                } else {
+                    ObjMesh mesh;
+                    try {
+                        mesh = LoadObj(base + local, smooth);
+                    } catch (const std::ios_base::failure& e) {
+                        throw SceneError(kErrIO, e.what());
+                    } catch (const ObjError& e) {
+                        throw SceneError(kErrParse, e.what());
                     }
-                scene->num_vertices += (int64_t)nv;
-                for (int64_t f = 0; f < prim.tri_count; f++) {
-                    for (int c = 0; c < 3; c++) {
-                        const uint32_t vi = mesh.faces[3 * f + c];
+                    prim.has_mesh = true;
+                    prim.has_uv = !mesh.texcoords.empty();
+                    prim.tri_first = scene->NumTriangles();
+                    prim.tri_count = (int64_t)(mesh.faces.size() / 3);
+                    const size_t nv = mesh.positions.size() / 3;
+                    for (size_t v = 0; v < nv; v++)
                         for (int k = 0; k < 3; k++) {
-                            scene->tri_pos.push_back((float)mesh.positions[3 * vi + k]);
-                            scene->tri_nrm.push_back((float)mesh.normals[3 * vi + k]);
+                            bmin[k] = std::fmin(bmin[k], mesh.positions[3 * v + k]);
+                            bmax[k] = std::fmax(bmax[k], mesh.positions[3 * v + k]);
                         }
-                        for (int k = 0; k < 2; k++)
-                            scene->tri_uv.push_back(prim.has_uv ? (float)mesh.texcoords[2 * vi + k] : 0.0f);
+                    scene->num_vertices += (int64_t)nv;
+                    for (int64_t f = 0; f < prim.tri_count; f++) {
+                        for (int c = 0; c < 3; c++) {
+                            const uint32_t vi = mesh.faces[3 * f + c];
+                            for (int k = 0; k < 3; k++) {
+                                scene->tri_pos.push_back((float)mesh.positions[3 * vi + k]);
+                                scene->tri_nrm.push_back((float)mesh.normals[3 * vi + k]);
+                            }
+                            for (int k = 0; k < 2; k++)
+                                scene->tri_uv.push_back(prim.has_uv ? (float)mesh.texcoords[2 * vi + k] : 0.0f);
+                        }
+                        scene->tri_prim.push_back((int32_t)scene->prims.size());
                     }
-                    scene->tri_prim.push_back((int32_t)scene->prims.size());
                 }
             }
 

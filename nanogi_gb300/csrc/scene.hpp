@@ -75,8 +75,22 @@ struct HostScene {
     int64_t NumTriangles() const { return (int64_t)tri_prim.size(); }
 };
 
-// Scene::Load (rt.hpp:1519-2154). Throws ngi::SceneError / YamlError / ObjError.
-std::unique_ptr<HostScene> LoadScene(const std::string& yaml_path, double aspect);
+// A caller-held indexed triangle mesh that replaces the file a primitive's `mesh: path:`
+// names (Mesh::Positions / Normals / Texcoords / Faces, rt.hpp:148-155).
+struct MemoryMesh {
+    std::string path;
+    const float* positions = nullptr;   // 3 per vertex
+    const float* normals = nullptr;     // 3 per vertex, or null: flat face normals
+    const float* texcoords = nullptr;   // 2 per vertex, or null
+    const uint32_t* faces = nullptr;    // 3 per triangle
+    int64_t num_vertices = 0;
+    int64_t num_triangles = 0;
+};
+
+// Scene::Load (rt.hpp:1519-2154). Throws ngi::SceneError / YamlError / ObjError. A mesh
+// path equal to the path of one of `memory` (verbatim) takes that mesh instead of a file.
+std::unique_ptr<HostScene> LoadScene(const std::string& yaml_path, double aspect,
+                                     const std::vector<MemoryMesh>* memory = nullptr);
 
 struct SceneError : std::runtime_error {
     int code;

@@ -351,15 +351,23 @@ def _yaml_scalar(x) -> str:
     return str(x)
 
 
-def write_scene(desc: SceneDesc, directory: str | os.PathLike, name: str = "scene.yml") -> Path:
+def _mesh_file(i: int, p: Primitive) -> str:
+    return f"{i:04d}_{p.name}.obj"
+
+
+def write_scene(desc: SceneDesc, directory: str | os.PathLike, name: str = "scene.yml",
+                write_meshes: bool = True) -> Path:
+    """Writes the YAML scene and, unless ``write_meshes`` is False, one OBJ per mesh. Without
+    the OBJ files the scene loads through ``Scene.load_with_meshes(path, a, memory_meshes(desc))``."""
     d = Path(directory)
     d.mkdir(parents=True, exist_ok=True)
     lines = ["version: 5", "scene:", "  primitives:"]
     for i, p in enumerate(desc.primitives):
         lines.append(f"    - type: [{', '.join(p.type)}]")
         if p.mesh is not None:
-            fn = f"{i:04d}_{p.name}.obj"
-            write_obj(d / fn, p.mesh, p.name)
+            fn = _mesh_file(i, p)
+            if write_meshes:
+                write_obj(d / fn, p.mesh, p.name)
             lines.append("      mesh:")
             lines.append(f"        path: '{fn}'")
         lines.append("      params:")
@@ -368,6 +376,12 @@ def write_scene(desc: SceneDesc, directory: str | os.PathLike, name: str = "scen
     path = d / name
     path.write_text("\n".join(lines) + "\n")
     return path
+
+
+def memory_meshes(desc: SceneDesc) -> dict:
+    """{mesh path in the YAML of write_scene: (positions, faces, normals, uvs)} for every mesh."""
+    return {_mesh_file(i, p): (p.mesh.positions, p.mesh.faces.astype(np.uint32), p.mesh.normals, p.mesh.uvs)
+            for i, p in enumerate(desc.primitives) if p.mesh is not None}
 
 
 WORKLOADS = {

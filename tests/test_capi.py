@@ -38,9 +38,10 @@ def test_struct_layouts_match_header(tmp_path):
     """Every ctypes field sits at the offset the C compiler gives the header's struct."""
     import subprocess
 
-    from nanogi_gb300.capi import RenderParams, RenderStats, SceneInfo
+    from nanogi_gb300.capi import BatchOptions, BatchStats, MeshData, RenderParams, RenderStats, SceneInfo
 
-    structs = {"ngi_render_params": RenderParams, "ngi_render_stats": RenderStats, "ngi_scene_info": SceneInfo}
+    structs = {"ngi_render_params": RenderParams, "ngi_render_stats": RenderStats, "ngi_scene_info": SceneInfo,
+               "ngi_batch_options": BatchOptions, "ngi_batch_stats": BatchStats, "ngi_mesh_data": MeshData}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "nanogi.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

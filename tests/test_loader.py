@@ -188,3 +188,47 @@ def test_directional_light_post_configuration(native_lib, tmp_path):
     assert info["num_lights"] == 3
     assert info["bound_min"] == pytest.approx([0, 0, 0], abs=1e-6)
     assert info["bound_max"] == pytest.approx([1, 1, 1], abs=1e-6)
+
+
+@pytest.mark.parametrize("workload", ["cornell_box", "material_box"])
+def test_memory_meshes_match_obj_files(native_lib, tmp_path, workload):
+    """ngi_scene_load_with_meshes flattens caller-held meshes exactly like their OBJ files."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    desc = scenegen.WORKLOADS[workload]()
+    a = _load(native_lib, scenegen.write_scene(desc, tmp_path / "files"))
+    b = ng.Scene.load_with_meshes(scenegen.write_scene(desc, tmp_path / "mem", write_meshes=False), 1.0,
+                                  scenegen.memory_meshes(desc))
+    for x, y in zip(a.triangles(), b.triangles()):
+        assert np.array_equal(x, y)
+    ia, ib = a.info(), b.info()
+    for k in ("num_triangles", "num_primitives", "num_lights", "sensor_index", "bound_min", "bound_max"):
+        assert np.array_equal(np.asarray(ia[k]), np.asarray(ib[k])), k
+
+
+def test_memory_mesh_flat_normals_and_errors(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    desc = scenegen.cornell_box()
+    path = scenegen.write_scene(desc, tmp_path, write_meshes=False)
+    mm = {k: (v[0], v[1], None, v[3]) for k, v in scenegen.memory_meshes(desc).items()}
+    s = ng.Scene.load_with_meshes(path, 1.0, mm)
+    P, N, _, _ = s.triangles()
+    P, N = P.reshape(-1, 3, 3).astype(np.float64), N.reshape(-1, 3, 3)
+    n = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    assert np.allclose(N, n[:, None, :], atol=1e-6)
+    bad = dict(mm)
+    k0 = next(iter(bad))
+    faces = bad[k0][1].copy()
+    faces[0, 0] = len(bad[k0][0])
+    bad[k0] = (bad[k0][0], faces)
+    with pytest.raises(ng.NanogiError) as e:
+        ng.Scene.load_with_meshes(path, 1.0, bad)
+    assert e.value.status == 1 and "out of range" in e.value.message
+    # a mesh missing from memory falls back to its (absent) file: an I/O error
+    del mm[k0]
+    with pytest.raises(ng.NanogiError):
+        ng.Scene.load_with_meshes(path, 1.0, mm)
