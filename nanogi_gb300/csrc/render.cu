@@ -163,6 +163,33 @@ NGI_D void film_add(double* film, uint32_t pixel, V3<R> c) {
 }
 
 // A pending shadow ray held in registers until the warp appends it.
+// Ray origins. REFERENCE: the surface point itself with the reference's absolute
+// tmin = EpsF (Scene::Intersect / Visible, rt.hpp:2248, 2260). SCALED: tmin = 0 and the point
+// moves off its surface, to the side the ray leaves by, by 2^-17 of the largest |coordinate|
+// of the surface triangle. Hit points are affine combinations of that triangle's vertices, so
+// their distance from its plane is a few ulps of that magnitude, and so is the error of a
+// later plane test against them; 2^-17 is 64..128 such ulps. The offset follows the local
+// geometry, not the scene, so millimetre triangles near the origin and kilometre walls both
+// stay clear of self-intersection. Shadow rays move both ends and run between the moved
+// points, stopping 2^-16 of their length short of the target.
+constexpr float kOffsetScale = 1.0f / 131072.0f;
+constexpr float kShadowShrink = 1.0f / 65536.0f;
+
+// g moved off its surface toward direction `toward` (unchanged off surfaces).
+template <typename R>
+NGI_D V3<R> offset_point(const Geom<R>& g, V3<R> toward) {
+    if (g.degenerated || !(g.ext > 0.0f)) return g.p;
+    const R delta = (R)(g.ext * kOffsetScale);
+    return g.p + g.gn * (dot(g.gn, toward) >= R(0) ? delta : -delta);
+}
+
+template <typename R>
+NGI_D float4 ray_origin(const Geom<R>& g, V3<R> d, int mode) {
+    if (mode != NGI_RAY_OFFSET_SCALED) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, kEpsF);
+    const V3<R> o = offset_point(g, d);
+    return make_float4((float)o.x, (float)o.y, (float)o.z, 0.0f);
+}
+
 template <typename R>
 struct ShadowRay {
     bool valid;
@@ -292,37 +319,29 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
         pix = (uint32_t)pixel_index(rx, ry, rc.width, rc.height);
     }
     // Scene::Visible (rt.hpp:2251-2261)
-    const V3<R> d = gl.p - g.p;
-    const R len = sqrt_(dot(d, d));
-    const V3<R> dn = d / len;
     out.valid = true;
-    const float4 ro = ray_origin(g, dn, rc.ray_offset);
-    out.ox = ro.x; out.oy = ro.y; out.oz = ro.z;
-    out.tmin = ro.w;
-    out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
-    out.tmax = (float)len * (1.0f - kEpsF);
+    if (rc.ray_offset == NGI_RAY_OFFSET_SCALED) {
+        const V3<R> a = offset_point(g, gl.p - g.p);
+        const V3<R> b = offset_point(gl, g.p - gl.p);
+        out.ox = (float)a.x; out.oy = (float)a.y; out.oz = (float)a.z;
+        const V3<R> d = b - v3<R>((R)out.ox, (R)out.oy, (R)out.oz);
+        const R len = sqrt_(dot(d, d));
+        const V3<R> dn = d / len;
+        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
+        out.tmin = 0.0f;
+        out.tmax = (float)len * (1.0f - kShadowShrink);
+    } else {
+        const V3<R> d = gl.p - g.p;
+        const R len = sqrt_(dot(d, d));
+        const V3<R> dn = d / len;
+        out.ox = (float)g.p.x; out.oy = (float)g.p.y; out.oz = (float)g.p.z;
+        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
+        out.tmin = kEpsF;
+        out.tmax = (float)len * (1.0f - kEpsF);
+    }
     out.c = C;
     out.pixel = pix;
     out.light_prim = L.prim;
-}
-
-// Float origin and tmin of a ray leaving surface point g in direction d. REFERENCE: the
-// reference's absolute tmin = EpsF (Scene::Intersect, rt.hpp:2248). SCALED: tmin = 0 and the
-// origin moves off the surface, to d's side of the geometric normal, by 2^-17 of the largest
-// |coordinate| of the surface triangle. The hit point is an affine combination of that
-// triangle's vertices, so its distance from the triangle's plane is a few ulps of that
-// magnitude, and so is the error of any later plane test against it; 2^-17 is 64..128 such
-// ulps. The offset grows with the local geometry, not with the scene, so millimetre
-// triangles near the origin and kilometre walls both keep clear of self-intersection.
-constexpr float kOffsetScale = 1.0f / 131072.0f;
-
-template <typename R>
-NGI_D float4 ray_origin(const Geom<R>& g, V3<R> d, int mode) {
-    if (mode != NGI_RAY_OFFSET_SCALED) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, kEpsF);
-    if (g.degenerated || !(g.ext > 0.0f)) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, 0.0f);
-    const R delta = (R)(g.ext * kOffsetScale);
-    const V3<R> o = g.p + g.gn * (dot(g.gn, d) >= R(0) ? delta : -delta);
-    return make_float4((float)o.x, (float)o.y, (float)o.z, 0.0f);
 }
 
 template <typename R>

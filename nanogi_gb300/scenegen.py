@@ -487,6 +487,134 @@ def inverse_box(seed: int = 5, emitter_seed: int = 7) -> SceneDesc:
 WORKLOADS["inverse_box"] = inverse_box
 
 
+def _sliver_face(rng, corner, eu, ev, normal, mu, sigma):
+    """Rectangle corner + [0,1] eu + [0,1] ev (|eu| >= |ev|) cut across ev into strips of two
+    long thin triangles each; every triangle's area is drawn log-normal(mu, sigma), the last
+    strip is clipped to the rectangle. Returns (positions (V,3), faces (F,3)) in float64."""
+    L = float(np.linalg.norm(eu))
+    S = float(np.linalg.norm(ev))
+    mean = math.exp(mu + 0.5 * sigma * sigma)
+    chunks, total = [], 0.0
+    while total < S:
+        w = 2.0 * rng.lognormal(mu, sigma, int(1.2 * S * L / (2.0 * mean)) + 8) / L
+        chunks.append(w)
+        total += float(w.sum())
+    cw = np.cumsum(np.concatenate(chunks))
+    k = int(np.searchsorted(cw, S))
+    f = np.concatenate([[0.0], np.minimum(cw[:k + 1], S)]) / S  # strip edges along ev
+    n = len(f) - 1
+    P = corner + f[:, None] * ev                                   # P_i on the corner edge
+    Q = P + eu                                                     # Q_i on the far edge
+    V = np.concatenate([P, Q])
+    i = np.arange(n)
+    F = np.concatenate([np.stack([i, n + 1 + i, n + 2 + i], 1), np.stack([i, n + 2 + i, i + 1], 1)])
+    if np.dot(np.cross(eu, ev), normal) < 0:
+        F = F[:, ::-1]
+    return V, F
+
+
+def precision_interior(num_triangles: int = 10_000_000, seed: int = 4, mu: float = -9.0, sigma: float = 2.5,
+                       light_le: float = 4.0e4) -> SceneDesc:
+    """The FP32-vs-FP64 precision workload: a furnished hall whose coordinates span 1e-3 to
+    1e3 scene units, built from long thin triangles.
+
+    * Hall: 2000 x 1000 x 2000 box (walls, ceiling), diffuse grey 0.4, facing in.
+    * Floor: graded square tiling around the origin, tiles h_k / 4 wide in the ring between
+      the squares of half-width h_(k-1) and h_k = 1000 / 2^(20-k): 9.5e-4 units next to the
+      origin, 250 units at the walls.
+    * Furniture: boxes of largest side s log-uniform in [1e-3, 2.4] (other sides s x U[0.15, 1]),
+      standing on the floor at distance s x 10^U[0.25, 1.4] from the origin, turned about y by
+      U[0, 180) degrees, in 4 diffuse albedo classes. Every face is cut into strips of two
+      long thin triangles with log-normal(mu, sigma) areas, until `num_triangles` in total.
+    * Light: one 0.05 x 0.05 quad emitter, 0.5 below a 60 x 60 white panel at height 3 and
+      facing it, so every path reaches the camera through at least one bounce.
+    """
+    rng = np.random.default_rng(seed)
+    s = SceneDesc()
+    # hall shell (inward normals)
+    H, W = 1000.0, 1000.0
+    shell = [quad((-W, 0, -W), (-W, H, -W), (-W, H, W), (-W, 0, W), (1, 0, 0)),
+             quad((W, 0, W), (W, H, W), (W, H, -W), (W, 0, -W), (-1, 0, 0)),
+             quad((W, 0, -W), (W, H, -W), (-W, H, -W), (-W, 0, -W), (0, 0, 1)),
+             quad((-W, 0, W), (-W, H, W), (W, H, W), (W, 0, W), (0, 0, -1)),
+             quad((-W, H, -W), (W, H, -W), (W, H, W), (-W, H, W), (0, -1, 0))]
+    t, p = diffuse((0.4, 0.4, 0.4))
+    s.primitives.append(Primitive(t, p, _merge(shell), "hall"))
+    # graded floor
+    tiles = []
+    h = [W / 2 ** (20 - k) for k in range(21)]
+    for k in range(21):
+        size = h[k] / 2 if k == 0 else h[k] / 4
+        n = 2 if k == 0 else 8
+        for a in range(n):
+            for b in range(n):
+                x0, z0 = -h[k] + a * size, -h[k] + b * size
+                if k > 0 and -h[k - 1] <= x0 < h[k - 1] and -h[k - 1] <= z0 < h[k - 1]:
+                    continue
+                tiles.append(quad((x0, 0, z0 + size), (x0 + size, 0, z0 + size), (x0 + size, 0, z0), (x0, 0, z0),
+                                  (0, 1, 0)))
+    t, p = diffuse((0.5, 0.5, 0.5))
+    s.primitives.append(Primitive(t, p, _merge(tiles), "floor"))
+    # reflector panel and the light under it
+    t, p = diffuse((0.8, 0.8, 0.8))
+    s.primitives.append(Primitive(t, p, quad((-30, 3, -30), (30, 3, -30), (30, 3, 30), (-30, 3, 30), (0, -1, 0)),
+                                  "panel"))
+    lt, lp = area_light((light_le, light_le, light_le))
+    lx, ly, lz, e = 0.4, 2.5, -0.6, 0.025
+    s.primitives.append(Primitive(lt, lp, quad((lx - e, ly, lz + e), (lx + e, ly, lz + e), (lx + e, ly, lz - e),
+                                               (lx - e, ly, lz - e), (0, 1, 0)), "light"))
+    eye = np.array([3.0, 2.2, 7.0])
+    # furniture
+    albedo = [(0.7, 0.55, 0.35), (0.75, 0.75, 0.72), (0.35, 0.38, 0.42), (0.6, 0.2, 0.15)]
+    parts = [([], []) for _ in albedo]
+    count = 0
+    unit_faces = [((-1, -1, 1), (1, 0, 0), (0, 1, 0), (0, 0, 1)), ((1, -1, -1), (-1, 0, 0), (0, 1, 0), (0, 0, -1)),
+                  ((1, -1, 1), (0, 0, -1), (0, 1, 0), (1, 0, 0)), ((-1, -1, -1), (0, 0, 1), (0, 1, 0), (-1, 0, 0)),
+                  ((-1, 1, 1), (1, 0, 0), (0, 0, -1), (0, 1, 0)), ((-1, -1, -1), (1, 0, 0), (0, 0, 1), (0, -1, 0))]
+    while count < num_triangles:
+        smax = 10 ** rng.uniform(-3.0, math.log10(2.4))
+        dims = smax * np.concatenate([[1.0], rng.uniform(0.15, 1.0, 2)])
+        dims = rng.permutation(dims)
+        r = smax * 10 ** rng.uniform(0.25, 1.4)
+        phi = rng.uniform(0, 2 * math.pi)
+        c = np.array([r * math.cos(phi), dims[1] / 2, r * math.sin(phi)])
+        if math.hypot(c[0] - eye[0], c[2] - eye[2]) < smax + 0.6:
+            continue
+        th = rng.uniform(0, math.pi)
+        rot = np.array([[math.cos(th), 0, math.sin(th)], [0, 1, 0], [-math.sin(th), 0, math.cos(th)]])
+        half = dims / 2
+        cls = int(rng.integers(len(albedo)))
+        for q0, du, dv, nn in unit_faces:
+            corner = c + rot @ (np.array(q0) * half)
+            eu = rot @ (np.array(du) * 2 * half)
+            ev = rot @ (np.array(dv) * 2 * half)
+            nrm = rot @ np.array(nn, np.float64)
+            if np.linalg.norm(eu) < np.linalg.norm(ev):
+                eu, ev = ev, eu
+            V, F = _sliver_face(rng, corner, eu, ev, nrm, mu, sigma)
+            parts[cls][0].append((V, nrm))
+            parts[cls][1].append(F)
+            count += len(F)
+    for cls, (vs, fs) in enumerate(parts):
+        if not vs:
+            continue
+        base = np.cumsum([0] + [len(v) for v, _ in vs[:-1]])
+        P = np.concatenate([v for v, _ in vs])
+        N = np.concatenate([np.broadcast_to(n, v.shape) for v, n in vs])
+        F = np.concatenate([f + b for f, b in zip(fs, base)])
+        t, p = diffuse(albedo[cls])
+        s.primitives.append(Primitive(t, p, Mesh(_f32(P), _f32(N), F.astype(np.int64)), f"furniture{cls}"))
+    s.primitives.append(pinhole(eye, (0.0, 0.2, 0.0), (0, 1, 0), 45.0))
+    return s
+
+
+def _merge(meshes) -> Mesh:
+    base = np.cumsum([0] + [len(m.positions) for m in meshes[:-1]])
+    uvs = [m.uvs if m.uvs is not None else np.zeros((len(m.positions), 2), np.float32) for m in meshes]
+    return Mesh(np.concatenate([m.positions for m in meshes]), np.concatenate([m.normals for m in meshes]),
+                np.concatenate([m.faces + b for m, b in zip(meshes, base)]), np.concatenate(uvs))
+
+
 def batch_jobs(num_jobs: int = 256, seed: int = 1000, pool_size: int = 160, max_tris: int = 200_000):
     """The batched-render workload: `num_jobs` independent jobs, each with a resolution drawn
     uniformly from {64^2, 128^2, 256^2, 512^2}, a triangle count log-uniform in 1k..max_tris,

@@ -3,6 +3,7 @@
     python -m nanogi_gb300.studies convergence [--ref-spp 8192]
     python -m nanogi_gb300.studies adjoint
     python -m nanogi_gb300.studies batch
+    python -m nanogi_gb300.studies precision [--ref-spp 1024]
 
 convergence: time to reach 1% relative RMSE against an FP64 reference, for the tuned path
 (FP32 shading) and the plain path (FP64 shading and path state), `pt` on the Cornell-box
@@ -84,6 +85,96 @@ def convergence(ref_spp: int = 8192, w: int = 256, h: int = 256, m: int = 8, max
         out["paths"][precision] = {"rungs": rungs, "spp_to_1pct": spp_1, "seconds_to_1pct": spp_1 * sec_per_spp,
                                    "seconds_per_spp": sec_per_spp}
     out["speedup_fp32_over_fp64"] = out["paths"]["fp64"]["seconds_to_1pct"] / out["paths"]["fp32"]["seconds_to_1pct"]
+    scene.close()
+    return out
+
+
+def precision(ref_spp: int = 1024, w: int = 1024, h: int = 1024, m: int = 32, num_triangles: int = 10_000_000,
+              max_rung_seconds: float = 20.0, bias_spp: int = 256):
+    """FP32-vs-FP64 study on the precision interior (scenegen.precision_interior): ~10M long
+    thin triangles, coordinates 1e-3..1e3, one small emitter seen only through bounces;
+    `ptdirect`, w x h, max path length m.
+
+    * Reference ("FP64 oracle"): the plain path -- FP64 shading, path state and film -- with
+      scaled ray offsets at ref_spp, rendered as two independent halves whose difference gives
+      its own noise, subtracted in quadrature from every error below.
+    * time to 1% rel-RMSE for the tuned FP32 path and the plain FP64 path (both scaled
+      offsets), extrapolated from a doubling spp ladder as in `convergence`.
+    * bias: FP32 (scaled offsets) and both paths with the reference's absolute tmin = 1e-4
+      against the FP64 reference, on 16 x 16-pixel block means, where noise averages out.
+    """
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    t0 = time.perf_counter()
+    desc = scenegen.precision_interior(num_triangles=num_triangles)
+    gen_s = time.perf_counter() - t0
+    d = tempfile.mkdtemp(prefix="ngi_precision_")
+    path = scenegen.write_scene(desc, d, write_meshes=False)
+    t0 = time.perf_counter()
+    scene = ng.Scene.load_with_meshes(path, w / h, scenegen.memory_meshes(desc))
+    load_s = time.perf_counter() - t0
+    del desc
+    t0 = time.perf_counter()
+    scene.build()
+    build_s = time.perf_counter() - t0
+    info = scene.info()
+
+    def render(precision, spp, seed, offset=0, ray_offset="scaled"):
+        r = ng.Renderer(renderer="ptdirect", num_samples=w * h * spp, max_num_vertices=m, width=w, height=h,
+                        seed=seed, sample_offset=offset, precision=precision, ray_offset=ray_offset)
+        f = r.render(scene)
+        st = r.last_stats
+        return f, st["render_ms"] / 1e3, st
+
+    half = ref_spp // 2
+    ra, ta, sta = render("fp64", half, 2024)
+    rb, tb, _ = render("fp64", half, 2024, offset=w * h * half)
+    ref = 0.5 * (ra + rb)
+    sigma_ref = rel_rmse(ra, rb) / 2.0
+    out = {"workload": f"precision_interior {info['num_triangles']} tris, {w}x{h}, ptdirect, max length {m}",
+           "scene": {"generate_seconds": gen_s, "load_seconds": load_s, "build_seconds": build_s,
+                     "bvh_nodes": info["bvh_nodes"], "bound_min": list(info["bound_min"]),
+                     "bound_max": list(info["bound_max"])},
+           "reference": {"precision": "fp64", "ray_offset": "scaled", "spp": ref_spp, "seconds": ta + tb,
+                         "rel_noise": sigma_ref,
+                         "mrays_per_s": (sta["extension_rays"] + sta["shadow_rays"]) / ta / 1e6},
+           "paths": {}}
+    for precision in ("fp32", "fp64"):
+        rungs = []
+        spp = 16
+        while True:
+            film, sec, st = render(precision, spp, 77)
+            err = rel_rmse(film, ref)
+            err_c = math.sqrt(max(err * err - sigma_ref * sigma_ref, 0.0))
+            rungs.append({"spp": spp, "seconds": sec, "rel_rmse": err, "rel_rmse_corrected": err_c,
+                          "mrays_per_s": (st["extension_rays"] + st["shadow_rays"]) / sec / 1e6,
+                          "msamples_per_s": w * h * spp / sec / 1e6})
+            if err_c < 0.01 or sec * 2 > max_rung_seconds or spp >= ref_spp:
+                break
+            spp *= 2
+        last = rungs[-1]
+        spp_1 = last["spp"] * (last["rel_rmse_corrected"] / 0.01) ** 2
+        sec_per_spp = last["seconds"] / last["spp"]
+        out["paths"][precision] = {"rungs": rungs, "spp_to_1pct": spp_1, "seconds_to_1pct": spp_1 * sec_per_spp,
+                                   "seconds_per_spp": sec_per_spp}
+    out["speedup_fp32_over_fp64"] = out["paths"]["fp64"]["seconds_to_1pct"] / out["paths"]["fp32"]["seconds_to_1pct"]
+
+    def blocks(x, b=16):
+        y = x.sum(2)
+        return y[: h // b * b, : w // b * b].reshape(h // b, b, w // b, b).mean((1, 3))
+
+    rb_ref = blocks(ref)
+    bias = {}
+    for precision, mode in (("fp32", "scaled"), ("fp32", "reference"), ("fp64", "reference")):
+        film, sec, _ = render(precision, bias_spp, 501, ray_offset=mode)
+        bias[f"{precision}/{mode}"] = {"spp": bias_spp, "image_mean_ratio": float(film.sum() / ref.sum()),
+                                       "block_rel_rmse": rel_rmse(blocks(film), rb_ref),
+                                       "rel_rmse": rel_rmse(film, ref)}
+    film, _, _ = render("fp64", bias_spp, 501)
+    bias["fp64/scaled (noise floor)"] = {"spp": bias_spp, "image_mean_ratio": float(film.sum() / ref.sum()),
+                                        "block_rel_rmse": rel_rmse(blocks(film), rb_ref), "rel_rmse": rel_rmse(film, ref)}
+    out["bias_vs_reference"] = bias
     scene.close()
     return out
 
@@ -182,7 +273,9 @@ def batch(num_jobs: int = 256):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["convergence", "adjoint", "batch"])
+    ap.add_argument("study", choices=["convergence", "adjoint", "batch", "precision"])
+    ap.add_argument("--triangles", type=int, default=10_000_000)
+    ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--ref-spp", type=int, default=8192)
     ap.add_argument("--max-ladder-spp", type=int, default=4096)
     a = ap.parse_args()
@@ -192,6 +285,8 @@ def main():
         print(json.dumps(adjoint_cost()), flush=True)
     elif a.study == "batch":
         print(json.dumps(batch()), flush=True)
+    elif a.study == "precision":
+        print(json.dumps(precision(a.ref_spp, a.res, a.res, num_triangles=a.triangles)), flush=True)
 
 
 if __name__ == "__main__":

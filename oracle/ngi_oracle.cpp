@@ -452,38 +452,52 @@ bool Intersect(const ora_scene& s, bool use_bvh, dv3 o, dv3 d, Isect& is, float 
     return true;
 }
 
+// Scaled ray offsets (not in the reference, which always uses tmin = EpsF, rt.hpp:2248):
+// a surface point moves 2^-17 x (largest |coordinate| of its triangle) along the geometric
+// normal, to the side the ray leaves by; tmin = 0. Shadow rays move both ends and stop 2^-16
+// of their length short of the moved target.
+dv3 OffsetPoint(const Geom& g, dv3 toward) {
+    if (g.degenerated || !(g.ext > 0.0f)) return g.p;
+    const double delta = (double)(g.ext * (1.0f / 131072.0f));
+    return g.p + g.gn * (dot(g.gn, toward) >= 0.0 ? delta : -delta);
+}
+
+dv3 ToFloat(dv3 v) { return dv3((float)v.x, (float)v.y, (float)v.z); }
+
 // Ray origin (a float point, held in doubles) and tmin for a ray leaving g toward d.
-// Mode 0 is the reference's absolute tmin = EpsF (rt.hpp:2248). Mode 1 (not in the
-// reference) uses tmin = 0 and moves the origin 2^-17 x (largest |coordinate| of the
-// surface triangle) along the geometric normal, to d's side.
 dv3 RayOrigin(const Geom& g, dv3 d, int mode, float& tmin) {
     if (mode != 1) {
         tmin = EpsF;
         return g.p;
     }
     tmin = 0.0f;
-    dv3 o = g.p;
-    if (!g.degenerated && g.ext > 0.0f) {
-        const double delta = (double)(g.ext * (1.0f / 131072.0f));
-        o = g.p + g.gn * (dot(g.gn, d) >= 0.0 ? delta : -delta);
-    }
-    return dv3((float)o.x, (float)o.y, (float)o.z);
+    return ToFloat(OffsetPoint(g, d));
 }
 
-// Scene::Visible (rt.hpp:2254-2262) from origin p1 with minimum distance tmin
-bool VisibleFrom(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2, dv3 d, float tmin) {
-    const double len = length(p2 - p1);
+// Visibility between two moved points (scaled offsets): tmin = 0, tmax short by 2^-16.
+bool VisibleBetween(const ora_scene& s, bool use_bvh, dv3 a, dv3 b) {
+    const dv3 v = b - a;
+    const double len = length(v);
+    const dv3 d = v / len;
+    const float of[3] = {(float)a.x, (float)a.y, (float)a.z};
+    const float df[3] = {(float)d.x, (float)d.y, (float)d.z};
+    const RayF r = MakeRay(of, df);
+    const float tmax = (float)len * (1.0f - 1.0f / 65536.0f);
+    const Hit h = use_bvh ? IntersectBvh(s, r, 0.0f, tmax, true) : IntersectBrute(s, r, 0.0f, tmax, true);
+    return h.tri < 0;
+}
+
+// Scene::Visible (rt.hpp:2254-2262)
+bool Visible(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2) {
+    const dv3 v = p2 - p1;
+    const double len = length(v);
+    const dv3 d = v / len;
     const float of[3] = {(float)p1.x, (float)p1.y, (float)p1.z};
     const float df[3] = {(float)d.x, (float)d.y, (float)d.z};
     const RayF r = MakeRay(of, df);
     const float tmax = (float)len * (1.0f - EpsF);
-    const Hit h = use_bvh ? IntersectBvh(s, r, tmin, tmax, true) : IntersectBrute(s, r, tmin, tmax, true);
+    const Hit h = use_bvh ? IntersectBvh(s, r, EpsF, tmax, true) : IntersectBrute(s, r, EpsF, tmax, true);
     return h.tri < 0;
-}
-
-bool Visible(const ora_scene& s, bool use_bvh, dv3 p1, dv3 p2) {
-    const dv3 v = p2 - p1;
-    return VisibleFrom(s, use_bvh, p1, p2, v / length(v), EpsF);
 }
 
 // ---- Primitive methods (rt.hpp:483-1466) ------------------------------------------------------
@@ -854,9 +868,13 @@ void ProcessSample(RenderCtx& c, Sampler& smp) {
             // Only trace the shadow ray when it can matter (same result as always tracing)
             if (!is_zero(Cpre * fsL)) {
                 c.sh++;
-                float tmin;
-                const dv3 o = RayOrigin(geom, ppL, P.ray_offset, tmin);
-                Vis = VisibleFrom(s, bvh, o, geomL.p, ppL, tmin) ? 1.0 : 0.0;
+                if (P.ray_offset == 1) {
+                    const dv3 a = ToFloat(OffsetPoint(geom, geomL.p - geom.p));
+                    const dv3 b = OffsetPoint(geomL, geom.p - geomL.p);
+                    Vis = VisibleBetween(s, bvh, a, b) ? 1.0 : 0.0;
+                } else {
+                    Vis = Visible(s, bvh, geom.p, geomL.p) ? 1.0 : 0.0;
+                }
             }
             const dv3 C = throughput * fsE * Gt * Vis * fsL * 1.0 / pdfL / pdfPL;
             if (!is_zero(C)) {

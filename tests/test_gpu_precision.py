@@ -1,0 +1,77 @@
+"""The precision workload on the GPU: long thin triangles whose coordinates span 1e-3..1e3.
+
+* The plain FP64 path with scaled ray offsets replays the oracle's render of a reduced
+  precision interior (same Philox paths; the oracle's own BVH, checked against brute force
+  elsewhere, to keep the CPU time short).
+* The tuned FP32 path agrees with it in expectation, and both offset modes agree on the
+  lamp-under-reflector geometry at unit scale.
+* The scene travels through ngi_scene_load_with_meshes, as the 10M-triangle study does.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_rmse
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_interior(native_lib, tmp_path_factory):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    desc = scenegen.precision_interior(num_triangles=40_000)
+    path = scenegen.write_scene(desc, tmp_path_factory.mktemp("interior"), write_meshes=False)
+    scene = ng.Scene.load_with_meshes(path, 1.0, scenegen.memory_meshes(desc))
+    yield desc, scene
+    scene.close()
+
+
+def test_fp64_scaled_offsets_replay_the_oracle(small_interior):
+    import nanogi_gb300 as ng
+    from oracle.oracle import OracleScene
+
+    desc, scene = small_interior
+    W = H = 32
+    n = W * H * 8
+    f = ng.Renderer(renderer="ptdirect", num_samples=n, max_num_vertices=8, width=W, height=H, seed=5,
+                    precision="fp64", ray_offset="scaled").render(scene)
+    ref = OracleScene.from_desc(desc, 1.0).render("ptdirect", num_samples=n, max_vertices=8, width=W, height=H,
+                                                  seed=5, rng_mode="replay", use_bvh=True, ray_offset="scaled")
+    assert ref.sum() > 0
+    close = np.isclose(f, ref, rtol=1e-6, atol=1e-9).all(2)
+    assert close.mean() > 0.99  # exact ties between overlapping slivers may break differently
+    assert rel_rmse(f, ref) < 1e-3
+
+
+def test_fp32_matches_fp64_in_expectation(small_interior):
+    import nanogi_gb300 as ng
+
+    _, scene = small_interior
+    W = H = 32
+    kw = dict(renderer="ptdirect", num_samples=W * H * 512, max_num_vertices=16, width=W, height=H,
+              ray_offset="scaled")
+    a = ng.Renderer(seed=1, precision="fp64", **kw).render(scene)
+    b = ng.Renderer(seed=2, precision="fp32", **kw).render(scene)
+    c = ng.Renderer(seed=3, precision="fp64", **kw).render(scene)
+    noise = rel_rmse(a, c)
+    assert rel_rmse(b, a) < 1.5 * noise
+    assert abs(b.sum() / a.sum() - 1) < 0.05
+
+
+def test_offset_modes_agree_under_the_reflector(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    d = scenegen.precision_interior(num_triangles=2000)
+    d.primitives = [p for p in d.primitives if not p.name.startswith("furniture") and p.name != "hall"]
+    for p in d.primitives:
+        if p.name == "light":
+            p.mesh.positions[:, 1] = 2.95
+    scene = ng.Scene.load(scenegen.write_scene(d, tmp_path), 1.0)
+    kw = dict(renderer="ptdirect", num_samples=32 * 32 * 64, max_num_vertices=4, width=32, height=32, seed=4)
+    a = ng.Renderer(ray_offset="scaled", **kw).render(scene)
+    b = ng.Renderer(ray_offset="reference", **kw).render(scene)
+    assert a.sum() > 0 and abs(a.sum() / b.sum() - 1) < 1e-3

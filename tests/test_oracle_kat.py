@@ -197,3 +197,42 @@ def test_scaled_ray_offsets_are_scale_invariant(oracle_lib):
         assert rel(f, unit) < 1e-4, scale
     big = OracleScene.from_desc(scenegen.transformed(base, 1e3), 1.0).render("ptdirect", **kw)
     assert big.sum() < 0.95 * unit.sum()  # shadow rays that hit their own surface
+
+
+def test_offset_modes_agree_on_a_light_under_a_reflector(oracle_lib):
+    """A small up-facing emitter close under a reflector panel (the precision workload's lamp):
+    shadow rays meet the panel at grazing angles, where moving only the shadow ray's origin
+    would let it hit the emitter itself. Both offset modes give the same image at unit scale."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    d = scenegen.precision_interior(num_triangles=2000)
+    d.primitives = [p for p in d.primitives if not p.name.startswith("furniture") and p.name != "hall"]
+    for p in d.primitives:
+        if p.name == "light":
+            p.mesh.positions[:, 1] = 2.95
+    o = OracleScene.from_desc(d, 1.0)
+    kw = dict(num_samples=24 * 24 * 32, max_vertices=4, width=24, height=24, seed=1)
+    a = o.render("ptdirect", ray_offset="scaled", **kw)
+    b = o.render("ptdirect", **kw)
+    assert a.sum() > 0
+    assert abs(a.sum() / b.sum() - 1) < 1e-3
+
+
+def test_precision_interior_statistics():
+    """Long thin triangles with log-normal(-9, 2.5) areas; coordinates from 1e-3 to 1e3."""
+    from nanogi_gb300 import scenegen
+
+    d = scenegen.precision_interior(num_triangles=60_000)
+    furn = [p for p in d.primitives if p.name.startswith("furniture")]
+    P = np.concatenate([p.mesh.positions[p.mesh.faces] for p in furn]).astype(np.float64)
+    area = 0.5 * np.linalg.norm(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), axis=1)
+    la = np.log(area[area > 0])
+    assert len(P) >= 60_000 and (area > 0).mean() > 0.98
+    assert abs(la.mean() + 9.0) < 0.1 and abs(la.std() - 2.5) < 0.1
+    longest = np.max([np.linalg.norm(P[:, i] - P[:, (i + 1) % 3], axis=1) for i in range(3)], 0)
+    assert np.median(longest ** 2 / (2 * area.clip(1e-30))) > 100  # long and thin
+    allp = np.concatenate([p.mesh.positions for p in d.primitives if p.mesh is not None])
+    mag = np.abs(allp[allp != 0])
+    assert mag.min() < 2e-3 and mag.max() == 1000.0
+    assert sum("L" in p.type for p in d.primitives) == 1
