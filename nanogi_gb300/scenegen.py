@@ -523,8 +523,9 @@ def precision_interior(num_triangles: int = 10_000_000, seed: int = 4, mu: float
       the squares of half-width h_(k-1) and h_k = 1000 / 2^(20-k): 9.5e-4 units next to the
       origin, 250 units at the walls.
     * Furniture: boxes of largest side s log-uniform in [1e-3, 2.4] (other sides s x U[0.15, 1]),
-      standing on the floor at distance s x 10^U[0.25, 1.4] from the origin, turned about y by
-      U[0, 180) degrees, in 4 diffuse albedo classes. Every face is cut into strips of two
+      standing on the floor at distance s x 10^U[0.25, 1.4] from the origin, aligned with the
+      hall (turned by 0 or 90 degrees) except one in ten turned by U[0, 180) degrees, in 4
+      diffuse albedo classes. Every face is cut into strips of two
       long thin triangles with log-normal(mu, sigma) areas, until `num_triangles` in total.
     * Light: one 0.05 x 0.05 quad emitter, 0.5 below a 60 x 60 white panel at height 3 and
       facing it, so every path reaches the camera through at least one bounce.
@@ -580,7 +581,8 @@ def precision_interior(num_triangles: int = 10_000_000, seed: int = 4, mu: float
         c = np.array([r * math.cos(phi), dims[1] / 2, r * math.sin(phi)])
         if math.hypot(c[0] - eye[0], c[2] - eye[2]) < smax + 0.6:
             continue
-        th = rng.uniform(0, math.pi)
+        # furniture follows the hall's grid, except one piece in ten
+        th = rng.uniform(0, math.pi) if rng.uniform() < 0.1 else 0.5 * math.pi * int(rng.integers(2))
         rot = np.array([[math.cos(th), 0, math.sin(th)], [0, 1, 0], [-math.sin(th), 0, math.cos(th)]])
         half = dims / 2
         cls = int(rng.integers(len(albedo)))

@@ -175,6 +175,16 @@ def precision(ref_spp: int = 1024, w: int = 1024, h: int = 1024, m: int = 32, nu
     bias["fp64/scaled (noise floor)"] = {"spp": bias_spp, "image_mean_ratio": float(film.sum() / ref.sum()),
                                         "block_rel_rmse": rel_rmse(blocks(film), rb_ref), "rel_rmse": rel_rmse(film, ref)}
     out["bias_vs_reference"] = bias
+    r = ng.Renderer(renderer="ptdirect", num_samples=w * h * 16, max_num_vertices=m, width=w, height=h, seed=9,
+                    ray_offset="scaled", flags=ng.capi.KERNEL_TIMING | ng.capi.TRAVERSAL_COUNTERS)
+    r.render(scene)
+    st = r.last_stats
+    out["traversal_fp32_16spp"] = {
+        "extend_nodes_per_ray": st["extend_nodes"] / max(st["extension_rays"], 1),
+        "extend_tris_per_ray": st["extend_tris"] / max(st["extension_rays"], 1),
+        "shadow_nodes_per_ray": st["shadow_nodes"] / max(st["shadow_rays"], 1),
+        "shadow_tris_per_ray": st["shadow_tris"] / max(st["shadow_rays"], 1),
+        "logic_ms": st["logic_ms"], "extend_ms": st["extend_ms"], "shadow_ms": st["shadow_ms"]}
     scene.close()
     return out
 
