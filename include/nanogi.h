@@ -50,7 +50,9 @@ typedef enum ngi_status {
 /* Renderer names of the reference (src/nanogi.cpp:51-69); only the path tracers are built. */
 typedef enum ngi_renderer_type {
     NGI_RENDERER_PT = 0,       /* "pt"       : ProcessSample_PT       src/nanogi.cpp:446-607 */
-    NGI_RENDERER_PTDIRECT = 1  /* "ptdirect" : ProcessSample_PTDirect src/nanogi.cpp:609-802 */
+    NGI_RENDERER_PTDIRECT = 1, /* "ptdirect" : ProcessSample_PTDirect src/nanogi.cpp:609-802 */
+    NGI_RENDERER_LT = 2,       /* "lt"       : ProcessSample_LT       src/nanogi.cpp:804-955 */
+    NGI_RENDERER_LTDIRECT = 3  /* "ltdirect" : ProcessSample_LTDirect src/nanogi.cpp:957-1131 */
 } ngi_renderer_type;
 
 /* Arithmetic of the shading stage. Traversal is FP32 and accumulation FP64 in both. */

@@ -54,8 +54,8 @@ ngi_status Guard(F&& f) {
 ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
     if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
     if (!p) return Fail(NGI_ERR_INVALID_ARGUMENT, "params is NULL");
-    if (p->renderer != NGI_RENDERER_PT && p->renderer != NGI_RENDERER_PTDIRECT)
-        return Fail(NGI_ERR_INVALID_ARGUMENT, "renderer must be pt or ptdirect");
+    if (p->renderer < NGI_RENDERER_PT || p->renderer > NGI_RENDERER_LTDIRECT)
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "renderer must be pt, ptdirect, lt or ltdirect");
     if (p->width <= 0 || p->height <= 0) return Fail(NGI_ERR_INVALID_ARGUMENT, "width and height must be positive");
     if ((int64_t)p->width * (int64_t)p->height > ((int64_t)1 << 31) - 1)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "width*height must fit in 31 bits");
@@ -75,6 +75,13 @@ ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
         return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_postpone must be 0 (auto) or 1..101");
     if (p->ray_offset != NGI_RAY_OFFSET_REFERENCE && p->ray_offset != NGI_RAY_OFFSET_SCALED)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "ray_offset must be REFERENCE or SCALED");
+    return NGI_OK;
+}
+
+// The batch, adjoint and allocation-free paths run the camera-path tracers only.
+ngi_status CheckCameraRenderer(const ngi_render_params* p) {
+    if (p->renderer != NGI_RENDERER_PT && p->renderer != NGI_RENDERER_PTDIRECT)
+        return Fail(NGI_ERR_UNSUPPORTED, "this entry point runs pt and ptdirect only");
     return NGI_OK;
 }
 
@@ -214,6 +221,7 @@ NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_
                                              void* stream) {
     const ngi_status st = CheckParams(scene, params);
     if (st != NGI_OK) return st;
+    if (CheckCameraRenderer(params) != NGI_OK) return NGI_ERR_UNSUPPORTED;
     if (!d_film_rgb) return Fail(NGI_ERR_INVALID_ARGUMENT, "film is NULL");
     return Guard([&]() {
         ngi::DeviceRenderNoAlloc(*scene->host, *params, d_film_rgb, (cudaStream_t)stream);
@@ -241,6 +249,7 @@ NGI_API ngi_status ngi_render_batch(ngi_scene* const* scenes, const ngi_render_p
     for (int32_t j = 0; j < num_jobs; j++) {
         const ngi_status st = CheckParams(scenes[j], &params[j]);
         if (st != NGI_OK) return Fail(st, "job " + std::to_string(j) + ": " + g_last_error);
+        if (CheckCameraRenderer(&params[j]) != NGI_OK) return NGI_ERR_UNSUPPORTED;
         hs[(size_t)j] = scenes[j]->host.get();
         ps[(size_t)j] = params[j];
     }
@@ -302,6 +311,7 @@ NGI_API ngi_status ngi_render_backward(ngi_scene* scene, const ngi_render_params
                                        double* grad_albedo, double* grad_emission) {
     const ngi_status st = CheckParams(scene, params);
     if (st != NGI_OK) return st;
+    if (CheckCameraRenderer(params) != NGI_OK) return NGI_ERR_UNSUPPORTED;
     if (!d_film) return Fail(NGI_ERR_INVALID_ARGUMENT, "d_film is NULL");
     return Guard([&]() {
         ngi::DeviceRenderBackward(*scene->host, *params, d_film, grad_albedo, grad_emission);

@@ -138,8 +138,10 @@ int main(int argc, char** argv) {
     const std::string r = o["renderer"].value;
     if (r == "pt") p.renderer = NGI_RENDERER_PT;
     else if (r == "ptdirect") p.renderer = NGI_RENDERER_PTDIRECT;
+    else if (r == "lt") p.renderer = NGI_RENDERER_LT;
+    else if (r == "ltdirect") p.renderer = NGI_RENDERER_LTDIRECT;
     else {
-        std::fprintf(stderr, "ERROR : renderer '%s' is not built (available: pt, ptdirect)\n", r.c_str());
+        std::fprintf(stderr, "ERROR : renderer '%s' is not built (available: pt, ptdirect, lt, ltdirect)\n", r.c_str());
         return EXIT_FAILURE;
     }
     try {

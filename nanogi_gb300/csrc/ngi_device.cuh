@@ -50,8 +50,9 @@ struct DevMaterial {
     R roughness;
     R eta1, eta2;  // S refraction / fresnel
     V3<R> Le;      // area light radiance (hit emission in pt)
+    V3<R> We;      // area sensor importance (hit with the sensor in lt)
     int light_index;
-    int pad;
+    int e_type;    // ET_* of a sensor primitive
 };
 
 // Light record (rt.hpp:389-416 + the area CDF of rt.hpp:1747-1765).

@@ -125,13 +125,22 @@ NGI_D R fresnel_dielectric(R cos_i, R eta_i, R eta_t) {
     return (rs * rs + rt * rt) * R(0.5);
 }
 
-// ---- BSDF evaluation, EL direction (rt.hpp:988-1140) ----------------------------------
+// Shading-normal correction factor (rt.hpp:994-1005): 0 where a direction lies on different
+// sides of the geometric and shading normals; otherwise 1 for EL (paths from the sensor) and
+// (wi.Ns wo.Ng) / (wo.Ns wi.Ng) for LE (paths from a light).
 template <typename R>
-NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, V3<R> wo, bool force_degenerated) {
-    const V3<R> lwi = to_local(g, wi), lwo = to_local(g, wo);
-    // shading-normal correction factor (rt.hpp:994-1005), EL: 1 or 0
+NGI_D R shading_correction(const Geom<R>& g, V3<R> wi, V3<R> wo, R lwi_z, R lwo_z, bool le) {
     const R wiNg = dot(wi, g.gn), woNg = dot(wo, g.gn);
-    const R corr = (wiNg * lwi.z <= R(0) || woNg * lwo.z <= R(0)) ? R(0) : R(1);
+    if (wiNg * lwi_z <= R(0) || woNg * lwo_z <= R(0)) return R(0);
+    return le ? (lwi_z * woNg) / (lwo_z * wiNg) : R(1);
+}
+
+// ---- BSDF evaluation (rt.hpp:988-1140); `le` selects the LE transport direction ----------
+template <typename R>
+NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, V3<R> wo, bool force_degenerated,
+                      bool le = false) {
+    const V3<R> lwi = to_local(g, wi), lwo = to_local(g, wo);
+    const R corr = shading_correction(g, wi, wo, lwi.z, lwo.z, le);
     const V3<R> zero = v3<R>(0, 0, 0);
     if (m.bsdf == BSDF_D) {
         if (lwi.z <= R(0) || lwo.z <= R(0)) return zero;
@@ -153,7 +162,7 @@ NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, V3<R>
         }
         R ei = m.eta1, et = m.eta2;
         if (lwi.z < R(0)) { const R t = ei; ei = et; et = t; }
-        const R eta = ei / et;
+        const R eta = le ? R(1) : ei / et;  // radiance scaling on refraction, EL only
         if (m.s_type == ST_REFRACTION) return m.R_ * (corr * eta * eta);
         const R Fr = fresnel_dielectric(lwi.z, ei, et);
         if (lwi.z * lwo.z >= R(0)) return m.R_ * (Fr * corr);
@@ -243,21 +252,21 @@ NGI_D bool bsdf_sample(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0
 // R*G*F*(wo.H)/(cos_i cos_H)*corr for G (no Beckmann exp); S keeps the explicit ratio.
 template <typename R>
 NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0, R u1, R ucomp, V3<R>& wo,
-                              V3<R>& weight) {
+                              V3<R>& weight, bool le = false) {
     if (!bsdf_sample(m, g, wi, u0, u1, ucomp, wo)) return false;
     if (m.bsdf == BSDF_S) {
-        const V3<R> fs = bsdf_eval(m, g, wi, wo, true);
+        const V3<R> fs = bsdf_eval(m, g, wi, wo, true, le);
         if (is_zero(fs)) return false;
         weight = fs / bsdf_pdf(m, g, wi, wo);
         return true;
     }
     const V3<R> lwi = to_local(g, wi), lwo = to_local(g, wo);
     if (lwi.z <= R(0) || lwo.z <= R(0)) return false;
-    const R wiNg = dot(wi, g.gn), woNg = dot(wo, g.gn);
-    if (wiNg * lwi.z <= R(0) || woNg * lwo.z <= R(0)) return false;  // shading-normal correction 0
+    const R corr = shading_correction(g, wi, wo, lwi.z, lwo.z, le);
+    if (corr == R(0)) return false;
     if (m.bsdf == BSDF_D) {
         if (is_zero(m.R_)) return false;
-        weight = m.R_;
+        weight = le ? m.R_ * corr : m.R_;
         return true;
     }
     // BSDF_G
@@ -265,7 +274,7 @@ NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> w
     if (H.z <= R(0) || beckmann_d(m.roughness, H) == R(0)) return false;
     const R G = shadow_masking(lwi, lwo, H);
     const V3<R> F = fr_conductor(m, dot(lwi, H));
-    weight = m.R_ * (G * dot(lwo, H) / (lwi.z * H.z)) * F;
+    weight = m.R_ * (G * dot(lwo, H) / (lwi.z * H.z) * (le ? corr : R(1))) * F;
     return !is_zero(weight);
 }
 
@@ -328,6 +337,56 @@ NGI_D void sample_mesh_position(const SceneView<R>& sv, int tri_base, int tri_co
     g.gn = normalize(cross(p2 - p1, p3 - p1));
     g.sn = g.gn;
     tangent_space(g);
+}
+
+// Primitive::SamplePosition for a light (rt.hpp:483-592): area mesh, point, or the disk of
+// the scene's bounding sphere that a directional light shines from.
+template <typename R>
+NGI_D void sample_light_position(const SceneView<R>& sv, const DevLight<R>& L, R u0, R u1, Geom<R>& g) {
+    g.uvx = g.uvy = R(0);
+    g.ext = 0.0f;
+    if (L.type == LT_AREA) {
+        sample_mesh_position(sv, L.tri_base, L.tri_count, L.cdf_offset, u0, u1, g);
+        return;
+    }
+    if (L.type == LT_POINT) {
+        g.p = L.position;
+        g.degenerated = true;
+        g.sn = g.gn = g.du = g.dv = v3<R>(0, 0, 0);
+        return;
+    }
+    R sx, sy;
+    concentric_disk(u0, u1, sx, sy);
+    g.degenerated = false;
+    g.gn = g.sn = L.direction;
+    tangent_space(g);
+    g.p = L.center - L.direction * L.radius + (g.du * (sx * L.radius) + g.dv * (sy * L.radius));
+}
+
+// Primitive::SampleDirection + EvaluateDirection(LE, forceDegenerated) / EvaluateDirectionPDF
+// for a light vertex (rt.hpp:697-714, 917-937, 1154-1171): the emitted direction and the
+// weight Le / pdf. False where the weight is zero.
+template <typename R>
+NGI_D bool light_sample_direction(const DevLight<R>& L, const Geom<R>& g, R u0, R u1, V3<R>& wo, V3<R>& weight) {
+    if (L.type == LT_AREA) {
+        const V3<R> l = cosine_hemisphere(u0, u1);
+        wo = to_world(g, l);
+        if (!(to_local(g, wo).z > R(0)) || is_zero(L.Le)) return false;
+        weight = L.Le / kInvPi_<R>();  // pdf 1/pi per projected solid angle
+        return true;
+    }
+    if (L.type == LT_POINT) {
+        const R z = R(1) - R(2) * u0;
+        const R r = sqrt_(fmax_(R(0), R(1) - z * z));
+        R sp, cp;
+        sincos2pi_(u1, &sp, &cp);
+        wo = v3<R>(r * cp, r * sp, z);
+        weight = L.Le / (kInvPi_<R>() * R(0.25));  // pdf 1/(4 pi) per solid angle
+        return !is_zero(L.Le);
+    }
+    wo = L.direction;
+    weight = L.Le;
+    return !is_zero(L.Le);
 }
 
 // GeometryTerm (rt.hpp:2364-2374)

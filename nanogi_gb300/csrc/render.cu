@@ -163,6 +163,15 @@ NGI_D void film_add(double* film, uint32_t pixel, V3<R> c) {
 }
 
 // A pending shadow ray held in registers until the warp appends it.
+template <typename R>
+struct ShadowRay {
+    bool valid;
+    float ox, oy, oz, dx, dy, dz, tmin, tmax;
+    V3<R> c;
+    uint32_t pixel;
+    int light_prim;  // adjoint: primitive whose Le scales the contribution
+};
+
 // Ray origins. REFERENCE: the surface point itself with the reference's absolute
 // tmin = EpsF (Scene::Intersect / Visible, rt.hpp:2248, 2260). SCALED: tmin = 0 and the point
 // moves off its surface, to the side the ray leaves by, by 2^-17 of the largest |coordinate|
@@ -183,6 +192,31 @@ NGI_D V3<R> offset_point(const Geom<R>& g, V3<R> toward) {
     return g.p + g.gn * (dot(g.gn, toward) >= R(0) ? delta : -delta);
 }
 
+// Scene::Visible (rt.hpp:2251-2261): the shadow ray from surface point a to b.
+template <typename R>
+NGI_D void shadow_segment(const Geom<R>& a, const Geom<R>& b, int mode, ShadowRay<R>& out) {
+    out.valid = true;
+    if (mode == NGI_RAY_OFFSET_SCALED) {
+        const V3<R> pa = offset_point(a, b.p - a.p);
+        const V3<R> pb = offset_point(b, a.p - b.p);
+        out.ox = (float)pa.x; out.oy = (float)pa.y; out.oz = (float)pa.z;
+        const V3<R> d = pb - v3<R>((R)out.ox, (R)out.oy, (R)out.oz);
+        const R len = sqrt_(dot(d, d));
+        const V3<R> dn = d / len;
+        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
+        out.tmin = 0.0f;
+        out.tmax = (float)len * (1.0f - kShadowShrink);
+    } else {
+        const V3<R> d = b.p - a.p;
+        const R len = sqrt_(dot(d, d));
+        const V3<R> dn = d / len;
+        out.ox = (float)a.p.x; out.oy = (float)a.p.y; out.oz = (float)a.p.z;
+        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
+        out.tmin = kEpsF;
+        out.tmax = (float)len * (1.0f - kEpsF);
+    }
+}
+
 template <typename R>
 NGI_D float4 ray_origin(const Geom<R>& g, V3<R> d, int mode) {
     if (mode != NGI_RAY_OFFSET_SCALED) return make_float4((float)g.p.x, (float)g.p.y, (float)g.p.z, kEpsF);
@@ -190,14 +224,6 @@ NGI_D float4 ray_origin(const Geom<R>& g, V3<R> d, int mode) {
     return make_float4((float)o.x, (float)o.y, (float)o.z, 0.0f);
 }
 
-template <typename R>
-struct ShadowRay {
-    bool valid;
-    float ox, oy, oz, dx, dy, dz, tmin, tmax;
-    V3<R> c;
-    uint32_t pixel;
-    int light_prim;  // adjoint: primitive whose Le scales the contribution
-};
 
 // Primitive id k of a path prefix held in two uint4 (16 x uint16).
 NGI_D uint32_t prefix_get(const uint4& a, const uint4& b, int k) {
@@ -318,27 +344,7 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
         }
         pix = (uint32_t)pixel_index(rx, ry, rc.width, rc.height);
     }
-    // Scene::Visible (rt.hpp:2251-2261)
-    out.valid = true;
-    if (rc.ray_offset == NGI_RAY_OFFSET_SCALED) {
-        const V3<R> a = offset_point(g, gl.p - g.p);
-        const V3<R> b = offset_point(gl, g.p - gl.p);
-        out.ox = (float)a.x; out.oy = (float)a.y; out.oz = (float)a.z;
-        const V3<R> d = b - v3<R>((R)out.ox, (R)out.oy, (R)out.oz);
-        const R len = sqrt_(dot(d, d));
-        const V3<R> dn = d / len;
-        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
-        out.tmin = 0.0f;
-        out.tmax = (float)len * (1.0f - kShadowShrink);
-    } else {
-        const V3<R> d = gl.p - g.p;
-        const R len = sqrt_(dot(d, d));
-        const V3<R> dn = d / len;
-        out.ox = (float)g.p.x; out.oy = (float)g.p.y; out.oz = (float)g.p.z;
-        out.dx = (float)dn.x; out.dy = (float)dn.y; out.dz = (float)dn.z;
-        out.tmin = kEpsF;
-        out.tmax = (float)len * (1.0f - kEpsF);
-    }
+    shadow_segment(g, gl, rc.ray_offset, out);
     out.c = C;
     out.pixel = pix;
     out.light_prim = L.prim;
@@ -360,6 +366,55 @@ NGI_D void store_ray(const WaveView<R>& w, int s, const Geom<R>& g, V3<R> d, int
 
 // BATCH: every slot belongs to one job of a batch; its scene, parameters, film and renderer
 // come from the device job table (one persistent wave serves every job).
+// Hit reconstruction (Scene::Intersect rt.hpp:2196-2233): the surface geometry where the ray
+// of slot s hit triangle h.w at distance h.x with barycentrics (h.y, h.z), the ray direction,
+// and the primitive hit. Scaled ray offsets place the point on the triangle (barycentric),
+// the reference mode at o + t d. Texture coordinates only when `with_uv` is set.
+template <typename R>
+NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const WaveView<R>& w, int s, float4 h, V3<R>& d,
+                       Geom<R>& g, bool with_uv) {
+    const int ti = __float_as_int(h.w);
+    V3<R> o;
+    if (sizeof(R) == 8) {
+        const Vec4T<double> a = w.od_o[s], b = w.od_d[s];
+        o = v3<R>((R)a.x, (R)a.y, (R)a.z);
+        d = v3<R>((R)b.x, (R)b.y, (R)b.z);
+    } else {
+        const float4 a = w.ray_o[s], b = w.ray_d[s];
+        o = v3<R>((R)a.x, (R)a.y, (R)a.z);
+        d = v3<R>((R)b.x, (R)b.y, (R)b.z);
+    }
+    const float4* tp = sv.tris + 3 * (size_t)ti;
+    const float4 q1 = tp[0], q2 = tp[1], q3 = tp[2];
+    const V3<R> p1 = v3<R>(q1.x, q1.y, q1.z), p2 = v3<R>(q2.x, q2.y, q2.z), p3 = v3<R>(q3.x, q3.y, q3.z);
+    g.gn = normalize(cross(p2 - p1, p3 - p1));
+    const float4* np = sv.nrm + 3 * (size_t)ti;
+    const float4 m1 = np[0], m2 = np[1], m3 = np[2];
+    const float bw = 1.0f - h.y - h.z;
+    if (rc.ray_offset == NGI_RAY_OFFSET_SCALED) {
+        // on the triangle itself, whatever the distance travelled
+        g.p = p1 * (R)bw + p2 * (R)h.y + p3 * (R)h.z;
+        g.ext = max_abs3(p1, p2, p3);
+    } else {
+        g.p = o + d * (R)h.x;
+        g.ext = 0.0f;
+    }
+    g.sn = normalize(v3<R>(m1.x, m1.y, m1.z) * (R)bw + v3<R>(m2.x, m2.y, m2.z) * (R)h.y +
+                     v3<R>(m3.x, m3.y, m3.z) * (R)h.z);
+    if (isnan_(g.sn.x) || isnan_(g.sn.y) || isnan_(g.sn.z)) g.sn = g.gn;
+    g.degenerated = false;
+    if (with_uv) {
+        const float2* up = sv.uv + 3 * (size_t)ti;
+        const float2 t1 = up[0], t2 = up[1], t3 = up[2];
+        g.uvx = (R)t1.x * (R)bw + (R)t2.x * (R)h.y + (R)t3.x * (R)h.z;
+        g.uvy = (R)t1.y * (R)bw + (R)t2.y * (R)h.y + (R)t3.y * (R)h.z;
+    } else {
+        g.uvx = R(0);
+        g.uvy = R(0);
+    }
+    return __float_as_int(m1.w);
+}
+
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false>
 __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
                                                const JobView<R>* __restrict__ jobs, int num_jobs) {
@@ -390,16 +445,9 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                 const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
                 double* const film = BATCH ? jobs[job].film : w.film;
                 const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
-                V3<R> o, d;
-                if (sizeof(R) == 8) {
-                    const Vec4T<double> a = w.od_o[s], b = w.od_d[s];
-                    o = v3<R>((R)a.x, (R)a.y, (R)a.z);
-                    d = v3<R>((R)b.x, (R)b.y, (R)b.z);
-                } else {
-                    const float4 a = w.ray_o[s], b = w.ray_d[s];
-                    o = v3<R>((R)a.x, (R)a.y, (R)a.z);
-                    d = v3<R>((R)b.x, (R)b.y, (R)b.z);
-                }
+                V3<R> d;
+                Geom<R> g;
+                const int prim = hit_geometry(sv, rc, w, s, h, d, g, false);
                 const Vec4T<R> t4 = w.thr[s];
                 V3<R> thr = v3<R>(t4.x, t4.y, t4.z);
                 const uint32_t pixel = w.pixel[s];
@@ -407,29 +455,6 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                 int nv = w.nverts[s];
                 const RngKey rk = make_rng(rc.seed, sample);
 
-                // Hit reconstruction (Scene::Intersect rt.hpp:2196-2233)
-                Geom<R> g;
-                const float4* tp = sv.tris + 3 * (size_t)ti;
-                const float4 q1 = tp[0], q2 = tp[1], q3 = tp[2];
-                const V3<R> p1 = v3<R>(q1.x, q1.y, q1.z), p2 = v3<R>(q2.x, q2.y, q2.z), p3 = v3<R>(q3.x, q3.y, q3.z);
-                g.gn = normalize(cross(p2 - p1, p3 - p1));
-                const float4* np = sv.nrm + 3 * (size_t)ti;
-                const float4 m1 = np[0], m2 = np[1], m3 = np[2];
-                const float bw = 1.0f - h.y - h.z;
-                if (rc.ray_offset == NGI_RAY_OFFSET_SCALED) {
-                    // on the triangle itself, whatever the distance travelled
-                    g.p = p1 * (R)bw + p2 * (R)h.y + p3 * (R)h.z;
-                    g.ext = max_abs3(p1, p2, p3);
-                } else {
-                    g.p = o + d * (R)h.x;
-                    g.ext = 0.0f;
-                }
-                g.sn = normalize(v3<R>(m1.x, m1.y, m1.z) * (R)bw + v3<R>(m2.x, m2.y, m2.z) * (R)h.y +
-                                 v3<R>(m3.x, m3.y, m3.z) * (R)h.z);
-                if (isnan_(g.sn.x) || isnan_(g.sn.y) || isnan_(g.sn.z)) g.sn = g.gn;
-                g.degenerated = false;
-                g.uvx = R(0); g.uvy = R(0);
-                const int prim = __float_as_int(m1.w);
                 const DevMaterial<R>& mat = sv.mats[prim];
                 if (ADJ) {
                     pa = w.pre[2 * (size_t)s];
@@ -644,6 +669,224 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
     if (ADJ && !DIRECT) adj_flush(w, gsm, rc0.num_prims);
 }
 
+// Direct sensor sampling of ltdirect (src/nanogi.cpp:1001-1051): connects vertex g -- a light
+// vertex when `light` is set, else a BSDF vertex of material `mat` reached from wi -- to a
+// position on the sensor, with the LE BSDF. The contribution is divided by the position pdf
+// of the path's light (`light_pos_pdf`), as the reference does (src/nanogi.cpp:1017 passes
+// the sampled sensor position to L->EvaluatePositionPDF): ltdirect images are the light
+// tracer's estimate scaled by that light's area.
+template <typename R>
+NGI_D void sensor_connect(const SceneView<R>& sv, const RenderConsts& rc, const Geom<R>& g, const DevLight<R>* light,
+                          const DevMaterial<R>* mat, V3<R> wi, V3<R> thr, R light_pos_pdf, float4 un,
+                          ShadowRay<R>& out) {
+    const DevSensor<R>& cam = sv.sensor;
+    Geom<R> ge;
+    if (cam.type == ET_PINHOLE) {
+        ge.p = cam.eye;
+        ge.degenerated = true;
+        ge.ext = 0.0f;
+        ge.sn = ge.gn = ge.du = ge.dv = v3<R>(0, 0, 0);
+        ge.uvx = ge.uvy = R(0);
+    } else {
+        sample_mesh_position(sv, cam.tri_base, cam.tri_count, cam.cdf_offset, (R)un.y, (R)un.z, ge);
+    }
+    const V3<R> ppe = normalize(ge.p - g.p);
+    V3<R> fs_l;
+    if (light) {
+        if (light->type == LT_DIRECTIONAL) return;  // Le is 0 without forceDegenerated (rt.hpp:934-937)
+        if (light->type == LT_AREA && !(to_local(g, ppe).z > R(0))) return;
+        fs_l = light->Le;
+    } else {
+        fs_l = bsdf_eval(*mat, g, wi, ppe, false, true);
+    }
+    if (is_zero(fs_l)) return;
+    V3<R> fs_e;
+    R rx = R(0), ry = R(0);
+    if (cam.type == ET_PINHOLE) {
+        const R W = pinhole_importance(cam, -ppe);
+        if (W == R(0)) return;
+        fs_e = v3<R>(W, W, W);
+        pinhole_raster(cam, -ppe, rx, ry);
+    } else {
+        if (!(dot(ge.sn, -ppe) > R(0))) return;
+        fs_e = cam.We;
+        rx = ge.uvx;
+        ry = ge.uvy;
+    }
+    const R G = geometry_term(g, ge);
+    const V3<R> C = thr * fs_l * G * fs_e / light_pos_pdf;
+    if (is_zero(C)) return;
+    shadow_segment(g, ge, rc.ray_offset, out);
+    out.c = C;
+    out.pixel = (uint32_t)pixel_index(rx, ry, rc.width, rc.height);
+    out.light_prim = -1;
+}
+
+// Position pdf of a light with forceDegenerated (rt.hpp:643-664).
+template <typename R>
+NGI_D R light_position_pdf(const DevLight<R>& L) {
+    return L.type == LT_POINT ? R(1) : L.inv_area;
+}
+
+// One wavefront step of the light tracers lt / ltdirect (ProcessSample_LT / _LTDirect,
+// src/nanogi.cpp:804-1131), the mirror of k_logic: paths start on a light picked uniformly,
+// leave it by its emission lobe and continue with LE BSDF sampling. lt scores where an
+// extension ray hits an area sensor; ltdirect connects every vertex, the light's own
+// included, to the sensor through a shadow ray. Random numbers per (sample, vertex):
+// RNG_SENSOR .z light pick, .xy position on it; RNG_NEE_RR .yz sensor position, .w Russian
+// roulette; RNG_DIR .xy direction, .z component choice.
+template <typename R, bool DIRECT>
+__global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
+        const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
+        uint8_t st = w.state[s];
+        bool need_new = st == SLOT_EMPTY;
+        bool want_ext = false;
+        ShadowRay<R> sa;
+        sa.valid = false;
+
+        if (st == SLOT_ACTIVE) {
+            bool alive = false;
+            const float4 h = w.hit[s];
+            if (__float_as_int(h.w) >= 0) {
+                V3<R> d;
+                Geom<R> g;
+                const int prim = hit_geometry(sv, rc, w, s, h, d, g, !DIRECT);
+                const DevMaterial<R>& mat = sv.mats[prim];
+                const Vec4T<R> t4 = w.thr[s];
+                V3<R> thr = v3<R>(t4.x, t4.y, t4.z);
+                const unsigned long long sample = w.sample[s];
+                int nv = w.nverts[s];
+                const RngKey rk = make_rng(rc.seed, sample);
+                if (!DIRECT && (mat.type & DT_E) && mat.e_type == ET_AREA) {
+                    // Hit with the sensor (src/nanogi.cpp:871-896): raster position = uv
+                    if (dot(g.sn, -d) > R(0)) {
+                        const V3<R> c = thr * mat.We;
+                        if (!is_zero(c)) {
+                            if (finite3(c)) {
+                                film_add(w.film, (uint32_t)pixel_index(g.uvx, g.uvy, rc.width, rc.height), c);
+                                atomicAdd(&w.ctr->stat_contrib, 1ull);
+                            } else {
+                                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                            }
+                        }
+                    }
+                }
+                // Russian roulette after every hit (src/nanogi.cpp:898-909)
+                const float rr = rng4(rk, (uint32_t)nv, RNG_NEE_RR).w;
+                if (!(rr > 0.5f)) {
+                    thr = thr / R(0.5);
+                    nv++;
+                    if (!(rc.max_vertices != -1 && nv >= rc.max_vertices) && mat.bsdf != BSDF_NONE) {
+                        tangent_space(g);
+                        const V3<R> wi = -d;
+                        if (DIRECT) {
+                            const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
+                            const R pdf_pe = light_position_pdf(sv.lights[w.pixel[s]]);
+                            sensor_connect(sv, rc, g, (const DevLight<R>*)nullptr, &mat, wi, thr, pdf_pe, un, sa);
+                        }
+                        const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
+                        V3<R> wo, wgt;
+                        if (bsdf_sample_weight(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo, wgt, true)) {
+                            thr = thr * wgt;
+                            store_ray(w, s, g, wo, rc.ray_offset);
+                            w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+                            w.nverts[s] = nv;
+                            alive = true;
+                            want_ext = true;
+                        }
+                    }
+                }
+            }
+            if (!alive) need_new = true;
+        }
+        {
+            const int q = warp_append(&w.ctr->sh_count, sa.valid);
+            if (sa.valid) {
+                w.sh_o[q] = make_float4(sa.ox, sa.oy, sa.oz, sa.tmin);
+                w.sh_d[q] = make_float4(sa.dx, sa.dy, sa.dz, sa.tmax);
+                w.sh_c[q] = Vec4T<R>{sa.c.x, sa.c.y, sa.c.z, R(0)};
+                w.sh_pix[q] = sa.pixel;
+            }
+        }
+
+        // ---- claim a new sample for finished slots: the light vertex ----
+        ShadowRay<R> sb;
+        sb.valid = false;
+        {
+            const unsigned mask = __ballot_sync(0xFFFFFFFFu, need_new);
+            unsigned long long k = 0;
+            if (mask != 0u) {
+                const int leader = __ffs(mask) - 1;
+                unsigned long long b = 0;
+                if ((int)lane_id() == leader) b = atomicAdd(&w.ctr->next_sample, (unsigned long long)__popc(mask));
+                b = __shfl_sync(0xFFFFFFFFu, b, leader);
+                k = b + (unsigned long long)__popc(mask & lanemask_lt());
+            }
+            if (need_new) {
+                if (k >= (unsigned long long)rc.num_samples) {
+                    st = SLOT_DONE;
+                } else if (rc.max_vertices == 1) {
+                    st = SLOT_EMPTY;  // the loop ends before the light vertex does anything
+                } else {
+                    const unsigned long long gsample = (unsigned long long)rc.sample_offset + k;
+                    const RngKey rk = make_rng(rc.seed, gsample);
+                    const float4 ul = rng4(rk, 1u, RNG_SENSOR);
+                    const int nl = sv.num_lights;
+                    int li = (int)((R)ul.z * (R)nl);
+                    li = li < 0 ? 0 : (li > nl - 1 ? nl - 1 : li);
+                    const DevLight<R>& L = sv.lights[li];
+                    Geom<R> gl;
+                    sample_light_position(sv, L, (R)ul.x, (R)ul.y, gl);
+                    const R pdf_pl = light_position_pdf(L);
+                    V3<R> thr = v3<R>(1, 1, 1) / pdf_pl / (R(1) / (R)nl);  // pdfL = 1 / #lights
+                    if (DIRECT) {
+                        const float4 un = rng4(rk, 1u, RNG_NEE_RR);
+                        sensor_connect(sv, rc, gl, &L, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, pdf_pl, un,
+                                       sb);
+                    }
+                    const float4 ud = rng4(rk, 1u, RNG_DIR);
+                    V3<R> wo, wgt;
+                    if (light_sample_direction(L, gl, (R)ud.x, (R)ud.y, wo, wgt)) {
+                        thr = thr * wgt;
+                        store_ray(w, s, gl, wo, rc.ray_offset);
+                        w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+                        w.pixel[s] = (uint32_t)li;  // the path's light (its position pdf scales ltdirect)
+                        w.sample[s] = gsample;
+                        w.nverts[s] = 1;
+                        want_ext = true;
+                        st = SLOT_ACTIVE;
+                    } else {
+                        st = SLOT_EMPTY;
+                    }
+                }
+            }
+            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+        }
+        if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
+        if (want_ext) st = SLOT_ACTIVE;
+        w.state[s] = st;
+        {
+            const int q = warp_append(&w.ctr->sh_count, sb.valid);
+            if (sb.valid) {
+                w.sh_o[q] = make_float4(sb.ox, sb.oy, sb.oz, sb.tmin);
+                w.sh_d[q] = make_float4(sb.dx, sb.dy, sb.dz, sb.tmax);
+                w.sh_c[q] = Vec4T<R>{sb.c.x, sb.c.y, sb.c.z, R(0)};
+                w.sh_pix[q] = sb.pixel;
+            }
+        }
+        {
+            const int q = warp_append(&w.ctr->ext_count, want_ext);
+            if (want_ext) w.ext_queue[q] = s;
+        }
+        {
+            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
+            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
+        }
+    }
+}
+
 // Adds a per-thread traversal count into a global counter with one atomic per warp.
 NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
     unsigned long long x = v;
@@ -833,6 +1076,8 @@ void build_tables(const HostScene& hs, std::vector<DevMaterial<R>>& mats, std::v
         m.eta1 = (R)p.S_eta1;
         m.eta2 = (R)p.S_eta2;
         m.Le = hv3<R>(p.Le);
+        m.We = hv3<R>(p.We);
+        m.e_type = p.e_type;
         m.light_index = -1;
         mats.push_back(m);
     }
@@ -1062,7 +1307,7 @@ struct TraceGrids {
     }
 };
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, bool LIGHT = false>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
                        int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev,
                        const JobView<R>* jobs = nullptr, int num_jobs = 0) {
@@ -1074,7 +1319,10 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
     const size_t adj_bytes = (ADJ && rc.num_prims <= kAdjSmemPrims) ? 6 * sizeof(float) * rc.num_prims : 0;
-    k_logic<R, DIRECT, ADJ, BATCH><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc, jobs, num_jobs);
+    if constexpr (LIGHT)
+        k_logic_lt<R, DIRECT><<<g_logic, 256, 0, stream>>>(sv, v, rc);
+    else
+        k_logic<R, DIRECT, ADJ, BATCH><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc, jobs, num_jobs);
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
     const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
@@ -1086,7 +1334,7 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, bool LIGHT = false>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
               bool kernel_timing, cudaStream_t stream, const JobView<R>* jobs = nullptr, int num_jobs = 0) {
     DeviceScene& ds = *hs.dev;
@@ -1104,8 +1352,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         cudaGraph_t graph = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < iters_per_graph; it++)
-            enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, nullptr, jobs,
-                                                            num_jobs);
+            enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LIGHT>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
+                                                                   nullptr, jobs, num_jobs);
         const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
         if (cap != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
@@ -1130,8 +1378,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
         while (true) {
             if (kernel_timing) {
-                enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH>(sv, v, rc, wv->ctr, g_logic, g_trace, stream, kev, jobs,
-                                                                num_jobs);
+                enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LIGHT>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
+                                                                       kev, jobs, num_jobs);
                 CUDA_CHECK(cudaGetLastError());
                 CUDA_CHECK(cudaEventSynchronize(kev[3]));
                 for (int k = 0; k < 3; k++) {
@@ -1192,8 +1440,8 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
     if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
-    if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
-        throw DeviceError("ptdirect needs at least one light (the reference indexes an empty light list)",
+    if (p.renderer != NGI_RENDERER_PT && ds.num_lights == 0)
+        throw DeviceError("this renderer needs at least one light (the reference indexes an empty light list)",
                           NGI_ERR_UNSUPPORTED);
     cudaStream_t stream = user_stream ? user_stream : ds.stream;
     ds.last_stats = ngi_render_stats{};
@@ -1221,8 +1469,21 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
-    const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
-    if (p.precision == NGI_PRECISION_FP64) {
+    const bool direct = p.renderer == NGI_RENDERER_PTDIRECT || p.renderer == NGI_RENDERER_LTDIRECT;
+    const bool light = p.renderer == NGI_RENDERER_LT || p.renderer == NGI_RENDERER_LTDIRECT;
+    if (light) {
+        if (p.precision == NGI_PRECISION_FP64) {
+            WaveView<double> v = wv->vd;
+            v.film = d_film;
+            if (direct) run_wave<double, true, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<double, false, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+        } else {
+            WaveView<float> v = wv->vf;
+            v.film = d_film;
+            if (direct) run_wave<float, true, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<float, false, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+        }
+    } else if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v = wv->vd;
         v.film = d_film;
         if (direct) run_wave<double, true, false>(hs, wv, v, rc, ipg, timing, stream);
@@ -1797,8 +2058,8 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
                           "nothing, so it cannot upload the scene)", NGI_ERR_INVALID_ARGUMENT);
     DeviceScene& ds = *hs.dev;
     if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
-    if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
-        throw DeviceError("ptdirect needs at least one light (the reference indexes an empty light list)",
+    if (p.renderer != NGI_RENDERER_PT && ds.num_lights == 0)
+        throw DeviceError("this renderer needs at least one light (the reference indexes an empty light list)",
                           NGI_ERR_UNSUPPORTED);
     if (p.flags != 0)
         throw DeviceError("measurement flags are not available on the allocation-free entry point",

@@ -928,6 +928,103 @@ void ProcessSample(RenderCtx& c, Sampler& smp) {
     }
 }
 
+// ProcessSample_LT / ProcessSample_LTDirect (src/nanogi.cpp:804-1131): paths start on a
+// light. lt scores only where an extension ray hits an area sensor; ltdirect connects every
+// vertex, the light's own included, to a sensor position. Random numbers: light pick and
+// position on (vertex 1, CALL_SENSOR); sensor pick and position of the connection on
+// (vertex, CALL_NEE_RR) lanes 0-2; direction on (vertex, CALL_DIR); Russian roulette on
+// (vertex, CALL_NEE_RR) lane 3 -- the reference's draw order in reference mode.
+void ProcessSampleLT(RenderCtx& c, Sampler& smp) {
+    const ora_scene& s = *c.s;
+    const ora_render_params& P = *c.p;
+    const bool direct = P.renderer == 3;
+    const bool bvh = P.use_bvh != 0;
+    std::vector<double>& film = *c.film;
+
+    // SampleEmitter(L, u), pdfL = 1 / #lights (rt.hpp:2321-2352)
+    const int n = (int)s.lights.size();
+    const double ul = smp.get(1, CALL_SENSOR, 2);
+    const int li = std::min(std::max((int)(ul * n), 0), n - 1);
+    const Prim& Lp = s.prims[s.lights[li]];
+    const double pdfL = 1.0 / n;
+    Geom geomL;
+    const double a0 = smp.get(1, CALL_SENSOR, 0), a1 = smp.get(1, CALL_SENSOR, 1);
+    SamplePosition(s, Lp, a0, a1, geomL);
+    const double pdfPL = PositionPdf(Lp);
+    dv3 throughput = dv3(1, 1, 1) / pdfPL / pdfL;  // EvaluatePosition(.., true) = 1
+    const Prim* prim = &Lp;
+    int type = L;
+    Geom geom = geomL;
+    dv3 wi(0, 0, 0);
+    int nv = 1;
+    c.cam++;
+    while (true) {
+        if (P.max_vertices != -1 && nv >= P.max_vertices) break;
+        if (direct) {
+            // Direct sensor sampling (src/nanogi.cpp:1001-1051)
+            smp.get(nv, CALL_NEE_RR, 0);  // SampleEmitter(E, u): the single sensor, pdfE = 1
+            const Prim& Ep = s.prims[s.sensor];
+            Geom geomE;
+            const double b0 = smp.get(nv, CALL_NEE_RR, 1), b1 = smp.get(nv, CALL_NEE_RR, 2);
+            SamplePosition(s, Ep, b0, b1, geomE);
+            // The reference divides by the LIGHT's position pdf here (src/nanogi.cpp:1017:
+            // L->EvaluatePositionPDF(geomE, true)), not the sensor's; kept for parity.
+            const double pdfPE = PositionPdf(Lp);
+            const dv3 ppE = normalize(geomE.p - geom.p);
+            const dv3 fsL = EvaluateDirection(*prim, geom, type, wi, ppE, true, false);
+            const dv3 fsE = EvaluateDirection(Ep, geomE, E, dv3(), -ppE, false, false);
+            const double Gt = GeometryTerm(geom, geomE);
+            const dv3 Cpre = throughput * fsL * Gt * fsE;
+            double Vis = 0.0;
+            if (!is_zero(Cpre)) {
+                c.sh++;
+                if (P.ray_offset == 1) {
+                    const dv3 a = ToFloat(OffsetPoint(geom, geomE.p - geom.p));
+                    const dv3 b = OffsetPoint(geomE, geom.p - geomE.p);
+                    Vis = VisibleBetween(s, bvh, a, b) ? 1.0 : 0.0;
+                } else {
+                    Vis = Visible(s, bvh, geom.p, geomE.p) ? 1.0 : 0.0;
+                }
+            }
+            const dv3 C = Cpre * Vis * 1.0 / 1.0 / pdfPE;  // x LeP = 1, / pdfE = 1
+            if (!is_zero(C)) {
+                double rx = 0, ry = 0;
+                RasterPosition(Ep, -ppE, geomE, rx, ry);
+                Accumulate(film, PixelIndex(rx, ry, P.width, P.height), C);
+            }
+        }
+        const double u0 = smp.get(nv, CALL_DIR, 0), u1 = smp.get(nv, CALL_DIR, 1);
+        const double ucomp = smp.get(nv, CALL_DIR, 2);
+        const dv3 wo = SampleDirection(*prim, u0, u1, ucomp, type, geom, wi);
+        const double pdfD = EvaluateDirectionPdf(*prim, geom, type, wi, wo);
+        const dv3 fs = EvaluateDirection(*prim, geom, type, wi, wo, true, true);
+        if (is_zero(fs)) break;
+        throughput = throughput * fs / pdfD;
+        Isect is;
+        c.ext++;
+        float tmin;
+        const dv3 ro = RayOrigin(geom, wo, P.ray_offset, tmin);
+        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) break;
+        const Prim& hp = s.prims[is.prim];
+        if (!direct && (hp.d.type & E)) {
+            // Hit with the sensor (src/nanogi.cpp:871-896)
+            double rx, ry;
+            if (!RasterPosition(hp, -wo, is.geom, rx, ry)) break;
+            const dv3 We = EvaluateDirection(hp, is.geom, E, dv3(), -wo, true, false);
+            Accumulate(film, PixelIndex(rx, ry, P.width, P.height), throughput * We);  // x EvaluatePosition = 1
+        }
+        const double rr = smp.get(nv, CALL_NEE_RR, 3);
+        if (rr > 0.5) break;
+        throughput = throughput / 0.5;
+        geom = is.geom;
+        prim = &hp;
+        type = hp.d.type & ~Emitter;
+        wi = -wo;
+        nv++;
+        if ((type & BSDF) == 0) break;
+    }
+}
+
 ora_scene* Build(const ora_prim_desc* prims, int n_prims, const float* tri_pos, const float* tri_nrm,
                  const float* tri_uv, int64_t n_tris, double aspect) {
     auto s = std::make_unique<ora_scene>();
@@ -1046,7 +1143,8 @@ int ora_visible(ora_scene* s, const double* pts, int64_t n, int32_t use_bvh, uin
 int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_render_stats* stats) {
     if (!s || !p || !film_out) { g_err = "NULL argument"; return 1; }
     if (s->sensor < 0) { g_err = "no sensor"; return 1; }
-    if (p->renderer == 1 && s->lights.empty()) { g_err = "ptdirect needs a light"; return 1; }
+    if (p->renderer < 0 || p->renderer > 3) { g_err = "unknown renderer"; return 1; }
+    if (p->renderer >= 1 && s->lights.empty()) { g_err = "this renderer needs a light"; return 1; }
     const size_t elems = 3 * (size_t)p->width * p->height;
     int threads = p->num_threads > 0 ? p->num_threads : (int)std::thread::hardware_concurrency();
     if (threads < 1) threads = 1;
@@ -1082,7 +1180,8 @@ int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_r
             for (int64_t k = b; k < e; k++) {
                 smp.sample = (uint64_t)(p->sample_offset + k);
                 smp.cache_vertex = 0xFFFFFFFFu;
-                ProcessSample(c, smp);
+                if (p->renderer >= 2) ProcessSampleLT(c, smp);
+                else ProcessSample(c, smp);
             }
         }
     };

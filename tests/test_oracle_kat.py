@@ -236,3 +236,34 @@ def test_precision_interior_statistics():
     mag = np.abs(allp[allp != 0])
     assert mag.min() < 2e-3 and mag.max() == 1000.0
     assert sum("L" in p.type for p in d.primitives) == 1
+
+
+def test_light_tracer_matches_path_tracer_on_an_area_sensor(oracle_lib):
+    """lt (src/nanogi.cpp:804-955) estimates the same image as pt when the sensor is an area
+    sensor the light paths can hit."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    o = OracleScene.from_desc(scenegen.area_sensor_box(), 1.0)
+    W = H = 8
+    kw = dict(num_samples=W * H * 4096, max_vertices=-1, width=W, height=H, rng_mode="reference")
+    pt = np.stack([o.render("ptdirect", seed=s, **kw) for s in (1, 2)])
+    lt = np.stack([o.render("lt", seed=s, **kw) for s in (3, 4)])
+    assert abs(lt.sum() / pt.sum() - 1) < 0.02
+    noise = np.sqrt(((pt[0] - pt[1]) ** 2).sum() / 2)
+    assert np.sqrt(((lt.mean(0) - pt.mean(0)) ** 2).sum()) < 3 * noise
+
+
+def test_ltdirect_keeps_the_reference_position_pdf(oracle_lib):
+    """ltdirect divides by the LIGHT's position pdf where the sensor's belongs
+    (src/nanogi.cpp:1017), so with a pinhole camera its image is ptdirect's times the area of
+    the (single) light: 0.25 x 0.25 in the Cornell box."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    o = OracleScene.from_desc(scenegen.cornell_box(), 1.0)
+    W = H = 8
+    kw = dict(num_samples=W * H * 4096, max_vertices=8, width=W, height=H, rng_mode="reference")
+    pt = o.render("ptdirect", seed=1, **kw)
+    ltd = o.render("ltdirect", seed=2, **kw)
+    assert ltd.sum() / pt.sum() == pytest.approx(0.0625, rel=0.02)
