@@ -301,6 +301,11 @@ NGI_API ngi_status ngi_save_image(const char* path, const double* film_rgb, int3
  * bottom (test helper; no reference counterpart beyond Texture::Load of .hdr, rt.hpp:168). */
 NGI_API ngi_status ngi_load_hdr(const char* path, double* film_rgb, int32_t width, int32_t height);
 
+/* Texture::Load (rt.hpp:167-256): decodes a TexR image (PNG 8-bit RGB/RGBA, PPM P6, BMP
+ * 24/32-bit, Radiance .hdr, PFM) into 3 floats per texel, row 0 = the image's top row, 8-bit
+ * values as v/255. With rgb == NULL only *width and *height are filled in. */
+NGI_API ngi_status ngi_load_texture(const char* path, float* rgb, int32_t* width, int32_t* height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -249,3 +249,13 @@ def load_hdr(path: str | os.PathLike, width: int, height: int) -> np.ndarray:
     film = np.empty((height, width, 3), np.float64)
     check(load_library().ngi_load_hdr(os.fsencode(str(path)), _ptr(film), width, height))
     return film
+
+
+def load_texture(path: str | os.PathLike) -> np.ndarray:
+    """A TexR image as (H, W, 3) float32, row 0 = the image's top row (Texture::Load)."""
+    lib = load_library()
+    w, h = ctypes.c_int32(), ctypes.c_int32()
+    check(lib.ngi_load_texture(os.fsencode(str(path)), None, ctypes.byref(w), ctypes.byref(h)))
+    img = np.empty((h.value, w.value, 3), np.float32)
+    check(lib.ngi_load_texture(os.fsencode(str(path)), _ptr(img), ctypes.byref(w), ctypes.byref(h)))
+    return img

@@ -21,7 +21,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["yaml_lite.cpp", "obj_loader.cpp", "scene.cpp", "image_io.cpp", "capi.cpp"]
+HOST_SOURCES = ["yaml_lite.cpp", "obj_loader.cpp", "scene.cpp", "image_io.cpp", "texture.cpp", "capi.cpp"]
 CUDA_SOURCES = ["render.cu", "bvh_build.cu"]
 LIB = OUT / "libnanogi.so"
 CLI = OUT / "nanogi"

@@ -158,6 +158,7 @@ PROTOTYPES = {
     "ngi_visible": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "ngi_save_image": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     "ngi_load_hdr": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    "ngi_load_texture": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, _P(ctypes.c_int32), _P(ctypes.c_int32)]),
 }
 
 _lib = None

@@ -10,6 +10,7 @@
 #include "../../include/nanogi.h"
 #include "device_scene.hpp"
 #include "image_io.hpp"
+#include "texture.hpp"
 #include "obj_loader.hpp"
 #include "scene.hpp"
 #include "yaml_lite.hpp"
@@ -312,6 +313,8 @@ NGI_API ngi_status ngi_render_backward(ngi_scene* scene, const ngi_render_params
     const ngi_status st = CheckParams(scene, params);
     if (st != NGI_OK) return st;
     if (CheckCameraRenderer(params) != NGI_OK) return NGI_ERR_UNSUPPORTED;
+    if (!scene->host->textures.empty())
+        return Fail(NGI_ERR_UNSUPPORTED, "the adjoint differentiates constant albedos; the scene has TexR textures");
     if (!d_film) return Fail(NGI_ERR_INVALID_ARGUMENT, "d_film is NULL");
     return Guard([&]() {
         ngi::DeviceRenderBackward(*scene->host, *params, d_film, grad_albedo, grad_emission);
@@ -350,6 +353,17 @@ NGI_API ngi_status ngi_load_hdr(const char* path, double* film_rgb, int32_t widt
     if (!path || !film_rgb || width <= 0 || height <= 0) return Fail(NGI_ERR_INVALID_ARGUMENT, "bad argument");
     return Guard([&]() {
         ngi::LoadHdr(path, film_rgb, width, height);
+        return NGI_OK;
+    });
+}
+
+NGI_API ngi_status ngi_load_texture(const char* path, float* rgb, int32_t* width, int32_t* height) {
+    if (!path || !width || !height) return Fail(NGI_ERR_INVALID_ARGUMENT, "NULL argument");
+    return Guard([&]() {
+        const ngi::TextureImage t = ngi::LoadTexture(path);
+        *width = t.width;
+        *height = t.height;
+        if (rgb) std::memcpy(rgb, t.rgb.data(), t.rgb.size() * sizeof(float));
         return NGI_OK;
     });
 }

@@ -174,8 +174,8 @@ int main(int argc, char** argv) {
         return EXIT_FAILURE;
     }
     const double render_time = std::atof(o["render-time"].value.c_str());
-    if (o["progress-image-update-interval"].set && std::atof(o["progress-image-update-interval"].value.c_str()) > 0)
-        std::fprintf(stderr, "WARN  : progress images are not written by this build\n");
+    const double image_interval = std::atof(o["progress-image-update-interval"].value.c_str());
+    const std::string image_format = o["progress-image-update-format"].value;
 
     std::fprintf(stderr, "nanogi-gb300\nLoading scene\n");
     ngi_scene* scene = nullptr;
@@ -188,12 +188,32 @@ int main(int argc, char** argv) {
     const auto t0 = std::chrono::steady_clock::now();
     ngi_status st = NGI_OK;
     long long processed = 0;
+    // Progress images (src/nanogi.cpp:356-404): after a batch of samples, when more than the
+    // interval has passed since the last one, the film so far goes to the format path with
+    // {{count}} replaced by the image count as %010d.
+    long long image_count = 0;
+    auto last_image = t0;
+    auto progress_image = [&](const std::vector<double>& f) {
+        if (!(image_interval > 0)) return;
+        const auto now = std::chrono::steady_clock::now();
+        if (std::chrono::duration<double>(now - last_image).count() <= image_interval) return;
+        char count[32];
+        std::snprintf(count, sizeof(count), "%010lld", ++image_count);
+        std::string path = image_format;
+        for (size_t at = path.find("{{count}}"); at != std::string::npos; at = path.find("{{count}}", at))
+            path.replace(at, 9, count);
+        std::fprintf(stderr, "Saving progress: %s\n", path.c_str());
+        if (ngi_save_image(path.c_str(), f.data(), p.width, p.height) != NGI_OK)
+            std::fprintf(stderr, "ERROR : %s\n", ngi_last_error());
+        last_image = now;
+    };
     if (render_time < 0) {
         st = ngi_render(scene, &p, film.data());
         processed = p.num_samples;
+        if (st == NGI_OK) progress_image(film);
     } else {
         // Time-budget mode (src/nanogi.cpp:243, 326-334): whole-image passes until time is up.
-        std::vector<double> part(film.size());
+        std::vector<double> part(film.size()), sum(film.size(), 0.0);
         ngi_render_params q = p;
         q.num_samples = (long long)p.width * p.height;
         while (st == NGI_OK) {
@@ -202,12 +222,13 @@ int main(int argc, char** argv) {
             if (st != NGI_OK) break;
             processed += q.num_samples;
             // part is normalised per pass; accumulate un-normalised sums
-            for (size_t k = 0; k < film.size(); k++) film[k] += part[k];
+            for (size_t k = 0; k < sum.size(); k++) sum[k] += part[k];
+            const double passes = (double)processed / q.num_samples;
+            for (size_t k = 0; k < film.size(); k++) film[k] = sum[k] / passes;
+            progress_image(film);
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > render_time) break;
         }
-        const double passes = (double)processed / q.num_samples;
-        for (auto& v : film) v /= passes;
     }
     const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (st != NGI_OK) {

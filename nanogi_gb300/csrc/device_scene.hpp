@@ -44,6 +44,9 @@ struct DeviceScene {
     double* cdf = nullptr;
     float* emit_pos = nullptr;
     float* emit_uv = nullptr;
+    float4* texels = nullptr;      // TexR images (see SceneView::texels)
+    int4* tex_info = nullptr;
+    int num_textures = 0;
     int num_lights = 0;
     // sensor records (host copies, passed by value to kernels)
     unsigned char sensor_f[256];

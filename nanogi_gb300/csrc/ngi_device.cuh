@@ -53,6 +53,8 @@ struct DevMaterial {
     V3<R> We;      // area sensor importance (hit with the sensor in lt)
     int light_index;
     int e_type;    // ET_* of a sensor primitive
+    int tex;       // TexR of the chosen D / G BSDF: index into SceneView::tex_info, -1 = the constant R_
+    int pad;
 };
 
 // Light record (rt.hpp:389-416 + the area CDF of rt.hpp:1747-1765).
@@ -100,6 +102,9 @@ struct SceneView {
     const double* cdf;         // FP64 emitter-area cdfs
     const float* emit_tri_pos; // 9 floats per emitter triangle (original order), light/sensor meshes
     const float* emit_tri_uv;  // 6 floats per emitter triangle
+    const float4* texels;      // TexR images, rgb + pad per texel, rows top first
+    const int4* tex_info;      // per texture: first texel, width, height
+    int num_textures;
     DevSensor<R> sensor;
 };
 

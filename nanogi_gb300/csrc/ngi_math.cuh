@@ -51,6 +51,8 @@ NGI_D float fmin_(float a, float b) { return fminf(a, b); }
 NGI_D double fmin_(double a, double b) { return fmin(a, b); }
 NGI_D float fabs_(float a) { return fabsf(a); }
 NGI_D double fabs_(double a) { return fabs(a); }
+NGI_D float floor_(float a) { return floorf(a); }
+NGI_D double floor_(double a) { return floor(a); }
 // sin / cos of 2*pi*u for u in [0,1)
 NGI_D void sincos2pi_(float u, float* s, float* c) { sincospif(2.0f * u, s, c); }
 NGI_D void sincos2pi_(double u, double* s, double* c) { sincospi(2.0 * u, s, c); }

@@ -135,16 +135,31 @@ NGI_D R shading_correction(const Geom<R>& g, V3<R> wi, V3<R> wo, R lwi_z, R lwo_
     return le ? (lwi_z * woNg) / (lwo_z * wiNg) : R(1);
 }
 
-// ---- BSDF evaluation (rt.hpp:988-1140); `le` selects the LE transport direction ----------
+// Albedo R of a D / G material at g: the texel of its TexR under g's uv -- nearest, with
+// fract wrap (Texture::Evaluate, rt.hpp:260-266) -- or the constant R.
 template <typename R>
-NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, V3<R> wo, bool force_degenerated,
-                      bool le = false) {
+NGI_D V3<R> material_albedo(const SceneView<R>& sv, const DevMaterial<R>& m, const Geom<R>& g) {
+    if (m.tex < 0) return m.R_;
+    const int4 t = sv.tex_info[m.tex];
+    const R fu = g.uvx - floor_(g.uvx), fv = g.uvy - floor_(g.uvy);
+    int x = (int)(fu * (R)t.y), y = (int)(fv * (R)t.z);
+    x = x < 0 ? 0 : (x > t.y - 1 ? t.y - 1 : x);
+    y = y < 0 ? 0 : (y > t.z - 1 ? t.z - 1 : y);
+    const float4 c = __ldg(sv.texels + t.x + (size_t)y * t.y + x);
+    return v3<R>((R)c.x, (R)c.y, (R)c.z);
+}
+
+// ---- BSDF evaluation (rt.hpp:988-1140); `le` selects the LE transport direction ----------
+// `albedo` is the R of D / G materials at this point (material_albedo); S uses m.R_.
+template <typename R>
+NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, V3<R> albedo, const Geom<R>& g, V3<R> wi, V3<R> wo,
+                      bool force_degenerated, bool le = false) {
     const V3<R> lwi = to_local(g, wi), lwo = to_local(g, wo);
     const R corr = shading_correction(g, wi, wo, lwi.z, lwo.z, le);
     const V3<R> zero = v3<R>(0, 0, 0);
     if (m.bsdf == BSDF_D) {
         if (lwi.z <= R(0) || lwo.z <= R(0)) return zero;
-        return m.R_ * (kInvPi_<R>() * corr);
+        return albedo * (kInvPi_<R>() * corr);
     }
     if (m.bsdf == BSDF_G) {
         if (lwi.z <= R(0) || lwo.z <= R(0)) return zero;
@@ -152,7 +167,7 @@ NGI_D V3<R> bsdf_eval(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, V3<R>
         const R D = beckmann_d(m.roughness, H);
         const R G = shadow_masking(lwi, lwo, H);
         const V3<R> F = fr_conductor(m, dot(lwi, H));
-        return m.R_ * (D * G) * F / (R(4) * lwi.z) / lwo.z * corr;
+        return albedo * (D * G) * F / (R(4) * lwi.z) / lwo.z * corr;
     }
     if (m.bsdf == BSDF_S) {
         if (!force_degenerated) return zero;
@@ -251,11 +266,11 @@ NGI_D bool bsdf_sample(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0
 // The ratio is formed in closed form where the lobe cancels: R*corr for D, and
 // R*G*F*(wo.H)/(cos_i cos_H)*corr for G (no Beckmann exp); S keeps the explicit ratio.
 template <typename R>
-NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> wi, R u0, R u1, R ucomp, V3<R>& wo,
-                              V3<R>& weight, bool le = false) {
+NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, V3<R> albedo, const Geom<R>& g, V3<R> wi, R u0, R u1, R ucomp,
+                              V3<R>& wo, V3<R>& weight, bool le = false) {
     if (!bsdf_sample(m, g, wi, u0, u1, ucomp, wo)) return false;
     if (m.bsdf == BSDF_S) {
-        const V3<R> fs = bsdf_eval(m, g, wi, wo, true, le);
+        const V3<R> fs = bsdf_eval(m, albedo, g, wi, wo, true, le);
         if (is_zero(fs)) return false;
         weight = fs / bsdf_pdf(m, g, wi, wo);
         return true;
@@ -265,8 +280,8 @@ NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> w
     const R corr = shading_correction(g, wi, wo, lwi.z, lwo.z, le);
     if (corr == R(0)) return false;
     if (m.bsdf == BSDF_D) {
-        if (is_zero(m.R_)) return false;
-        weight = le ? m.R_ * corr : m.R_;
+        if (is_zero(albedo)) return false;
+        weight = le ? albedo * corr : albedo;
         return true;
     }
     // BSDF_G
@@ -274,7 +289,7 @@ NGI_D bool bsdf_sample_weight(const DevMaterial<R>& m, const Geom<R>& g, V3<R> w
     if (H.z <= R(0) || beckmann_d(m.roughness, H) == R(0)) return false;
     const R G = shadow_masking(lwi, lwo, H);
     const V3<R> F = fr_conductor(m, dot(lwi, H));
-    weight = m.R_ * (G * dot(lwo, H) / (lwi.z * H.z) * (le ? corr : R(1))) * F;
+    weight = albedo * (G * dot(lwo, H) / (lwi.z * H.z) * (le ? corr : R(1))) * F;
     return !is_zero(weight);
 }
 

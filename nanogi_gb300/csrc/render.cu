@@ -325,7 +325,7 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
             fs_e = dot(g.sn, ppl) > R(0) ? sv.sensor.We : v3<R>(0, 0, 0);
         }
     } else {
-        fs_e = bsdf_eval(*mat, g, wi, ppl, false);
+        fs_e = bsdf_eval(*mat, material_albedo(sv, *mat, g), g, wi, ppl, false);
     }
     if (is_zero(fs_e)) return;
     V3<R> fs_l = L.Le;
@@ -403,7 +403,7 @@ NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const Wav
                      v3<R>(m3.x, m3.y, m3.z) * (R)h.z);
     if (isnan_(g.sn.x) || isnan_(g.sn.y) || isnan_(g.sn.z)) g.sn = g.gn;
     g.degenerated = false;
-    if (with_uv) {
+    if (with_uv || sv.num_textures > 0) {
         const float2* up = sv.uv + 3 * (size_t)ti;
         const float2 t1 = up[0], t2 = up[1], t3 = up[2];
         g.uvx = (R)t1.x * (R)bw + (R)t2.x * (R)h.y + (R)t3.x * (R)h.z;
@@ -492,7 +492,8 @@ __global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, 
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
                         V3<R> wo, wgt;
-                        if (bsdf_sample_weight(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo, wgt)) {
+                        if (bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y, (R)ud.z,
+                                               wo, wgt)) {
                             {
                                 thr = thr * wgt;
                                 if (ADJ) {
@@ -697,7 +698,7 @@ NGI_D void sensor_connect(const SceneView<R>& sv, const RenderConsts& rc, const 
         if (light->type == LT_AREA && !(to_local(g, ppe).z > R(0))) return;
         fs_l = light->Le;
     } else {
-        fs_l = bsdf_eval(*mat, g, wi, ppe, false, true);
+        fs_l = bsdf_eval(*mat, material_albedo(sv, *mat, g), g, wi, ppe, false, true);
     }
     if (is_zero(fs_l)) return;
     V3<R> fs_e;
@@ -788,7 +789,8 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
                         V3<R> wo, wgt;
-                        if (bsdf_sample_weight(mat, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo, wgt, true)) {
+                        if (bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y, (R)ud.z,
+                                               wo, wgt, true)) {
                             thr = thr * wgt;
                             store_ray(w, s, g, wo, rc.ray_offset);
                             w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
@@ -1078,6 +1080,7 @@ void build_tables(const HostScene& hs, std::vector<DevMaterial<R>>& mats, std::v
         m.Le = hv3<R>(p.Le);
         m.We = hv3<R>(p.We);
         m.e_type = p.e_type;
+        m.tex = m.bsdf == BSDF_D ? p.D_tex : (m.bsdf == BSDF_G ? p.G_tex : -1);
         m.light_index = -1;
         mats.push_back(m);
     }
@@ -1134,6 +1137,9 @@ SceneView<R> make_view(const DeviceScene& ds) {
     v.cdf = ds.cdf;
     v.emit_tri_pos = ds.emit_pos;
     v.emit_tri_uv = ds.emit_uv;
+    v.texels = ds.texels;
+    v.tex_info = ds.tex_info;
+    v.num_textures = ds.num_textures;
     std::memcpy(&v.sensor, sizeof(R) == 8 ? ds.sensor_d : ds.sensor_f, sizeof(DevSensor<R>));
     return v;
 }
@@ -1190,6 +1196,18 @@ void DeviceUpload(HostScene& hs) {
         ds->cdf = upload<double>(cdf.data(), cdf.size());
         ds->emit_pos = upload<float>(epos.data(), epos.size());
         ds->emit_uv = upload<float>(euv.data(), euv.size());
+        if (!hs.textures.empty()) {
+            std::vector<int4> info;
+            std::vector<float4> texels;
+            for (const TextureImage& t : hs.textures) {
+                info.push_back(make_int4((int)texels.size(), t.width, t.height, 0));
+                for (size_t i = 0; i < (size_t)t.width * t.height; i++)
+                    texels.push_back(make_float4(t.rgb[3 * i], t.rgb[3 * i + 1], t.rgb[3 * i + 2], 0.0f));
+            }
+            ds->tex_info = upload<int4>(info.data(), info.size());
+            ds->texels = upload<float4>(texels.data(), texels.size());
+            ds->num_textures = (int)info.size();
+        }
         ds->num_lights = (int)lf.size();
         std::memcpy(ds->sensor_f, &sf, sizeof(sf));
         std::memcpy(ds->sensor_d, &sd, sizeof(sd));
@@ -1206,7 +1224,8 @@ void DeviceFree(HostScene& hs) {
     if (ds->stream) cudaStreamSynchronize(ds->stream);
     free_wave(ds->wave);
     void* ptrs[] = {ds->nodes, ds->tris, ds->nrm, ds->uv, ds->mats_f, ds->mats_d, ds->lights_f,
-                    ds->lights_d, ds->cdf, ds->emit_pos, ds->emit_uv, ds->film, ds->adj, ds->grads};
+                    ds->lights_d, ds->cdf, ds->emit_pos, ds->emit_uv, ds->texels, ds->tex_info, ds->film,
+                    ds->adj, ds->grads};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (ds->stream) cudaStreamDestroy(ds->stream);

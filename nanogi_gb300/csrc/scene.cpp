@@ -5,7 +5,9 @@
 #include <cmath>
 #include <fstream>
 
+#include "image_io.hpp"
 #include "obj_loader.hpp"
+#include "texture.hpp"
 #include "yaml_lite.hpp"
 
 namespace ngi {
@@ -130,6 +132,21 @@ std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect, con
     auto scene = std::make_unique<HostScene>();
     scene->path = path;
     const std::string base = ParentDir(path);
+    // LoadTexture (rt.hpp:1775-1802): one image per distinct path, relative to the scene file.
+    // A texture that does not load fails the scene (the reference logs it and renders black).
+    std::vector<std::string> texture_paths;
+    auto load_texture = [&](const std::string& local) -> int {
+        const std::string tp = base + local;
+        for (size_t i = 0; i < texture_paths.size(); i++)
+            if (texture_paths[i] == tp) return (int)i;
+        try {
+            scene->textures.push_back(LoadTexture(tp));
+        } catch (const ImageError& e) {
+            throw SceneError(e.code, e.what());
+        }
+        texture_paths.push_back(tp);
+        return (int)texture_paths.size() - 1;
+    };
 
     try {
         const YamlNode& doc = *root;
@@ -270,7 +287,7 @@ std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect, con
                 if (D.Has("R")) {
                     ParseVec3(D["R"], prim.D_R, where + " D.R");
                 } else if (D.Has("TexR")) {
-                    throw SceneError(kErrUnsupported, where + ": D.TexR textures are not supported yet");
+                    prim.D_tex = load_texture(D["TexR"].AsString());
                 } else {
                     throw SceneError(kErrParse, where + ": D needs R");
                 }
@@ -283,7 +300,7 @@ std::unique_ptr<HostScene> LoadScene(const std::string& path, double aspect, con
                 if (G.Has("R")) {
                     ParseVec3(G["R"], prim.G_R, where + " G.R");
                 } else if (G.Has("TexR")) {
-                    throw SceneError(kErrUnsupported, where + ": G.TexR textures are not supported yet");
+                    prim.G_tex = load_texture(G["TexR"].AsString());
                 } else {
                     throw SceneError(kErrParse, where + ": G needs R");
                 }

@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include "texture.hpp"
+
 namespace ngi {
 
 // PrimitiveType bits (rt.hpp:338-351).
@@ -44,8 +46,10 @@ struct HostPrimitive {
 
     // D
     double D_R[3] = {0, 0, 0};
+    int D_tex = -1;                 // TexR: index into HostScene::textures, -1 = the constant R
     // G
     double G_R[3] = {0, 0, 0}, G_eta[3] = {0, 0, 0}, G_k[3] = {0, 0, 0};
+    int G_tex = -1;
     double G_roughness = 0;
     // S
     int s_type = S_REFLECTION;
@@ -67,6 +71,7 @@ struct HostScene {
     std::vector<float> tri_nrm;     // 9 per triangle (n1, n2, n3)
     std::vector<float> tri_uv;      // 6 per triangle (zeros when the mesh has none)
     std::vector<int32_t> tri_prim;  // owning primitive
+    std::vector<TextureImage> textures;  // TexR images (Scene::Textures, rt.hpp:1495)
     int64_t num_vertices = 0;
     double bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
 

@@ -48,6 +48,9 @@ class Primitive:
 @dataclass
 class SceneDesc:
     primitives: list[Primitive] = field(default_factory=list)
+    # TexR images by file name: (H, W, 3) float32, row 0 = the image's top row. 8-bit formats
+    # hold multiples of 1/255 so the file stores them exactly.
+    textures: dict = field(default_factory=dict)
 
     @property
     def num_triangles(self) -> int:
@@ -351,6 +354,70 @@ def _yaml_scalar(x) -> str:
     return str(x)
 
 
+# ---- texture files (the images TexR names) --------------------------------------------------
+def _png_bytes(img8: np.ndarray) -> bytes:
+    """8-bit RGB PNG; the rows cycle through the five filter types."""
+    import struct
+    import zlib
+
+    h, w, _ = img8.shape
+    stride = 3 * w
+    prev = np.zeros(stride, np.int32)
+    raw = bytearray()
+    for y in range(h):
+        cur = img8[y].reshape(-1).astype(np.int32)
+        a = np.concatenate([np.zeros(3, np.int32), cur[:-3]])
+        c = np.concatenate([np.zeros(3, np.int32), prev[:-3]])
+        ft = y % 5
+        if ft == 0:
+            out = cur
+        elif ft == 1:
+            out = cur - a
+        elif ft == 2:
+            out = cur - prev
+        elif ft == 3:
+            out = cur - (a + prev) // 2
+        else:
+            p = a + prev - c
+            pa, pb, pc = np.abs(p - a), np.abs(p - prev), np.abs(p - c)
+            pred = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, prev, c))
+            out = cur - pred
+        raw.append(ft)
+        raw += (out % 256).astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+            + chunk(b"IDAT", zlib.compress(bytes(raw), 9)) + chunk(b"IEND", b""))
+
+
+def write_texture(path: Path, img: np.ndarray) -> None:
+    """Writes a TexR image as .png / .ppm / .bmp (8-bit) or .pfm (float), top row first."""
+    import struct
+
+    img = np.asarray(img, np.float32)
+    h, w, _ = img.shape
+    ext = Path(path).suffix
+    if ext == ".pfm":
+        Path(path).write_bytes(f"PF\n{w} {h}\n-1.0\n".encode() + img[::-1].astype("<f4").tobytes())
+        return
+    img8 = np.rint(img * 255.0).astype(np.uint8)
+    if ext == ".png":
+        Path(path).write_bytes(_png_bytes(img8))
+    elif ext == ".ppm":
+        Path(path).write_bytes(f"P6\n# nanogi texture\n{w} {h}\n255\n".encode() + img8.tobytes())
+    elif ext == ".bmp":
+        stride = (3 * w + 3) & ~3
+        rows = b"".join(img8[y, :, ::-1].tobytes() + b"\0" * (stride - 3 * w) for y in range(h - 1, -1, -1))
+        header = struct.pack("<2sIHHI", b"BM", 54 + len(rows), 0, 0, 54)
+        dib = struct.pack("<IiiHHIIiiII", 40, w, h, 1, 24, 0, len(rows), 2835, 2835, 0, 0)
+        Path(path).write_bytes(header + dib + rows)
+    else:
+        raise ValueError(f"no writer for {ext}")
+
+
 def _mesh_file(i: int, p: Primitive) -> str:
     return f"{i:04d}_{p.name}.obj"
 
@@ -361,6 +428,8 @@ def write_scene(desc: SceneDesc, directory: str | os.PathLike, name: str = "scen
     the OBJ files the scene loads through ``Scene.load_with_meshes(path, a, memory_meshes(desc))``."""
     d = Path(directory)
     d.mkdir(parents=True, exist_ok=True)
+    for tex_name, img in desc.textures.items():
+        write_texture(d / tex_name, img)
     lines = ["version: 5", "scene:", "  primitives:"]
     for i, p in enumerate(desc.primitives):
         lines.append(f"    - type: [{', '.join(p.type)}]")
@@ -428,13 +497,42 @@ def area_sensor_box() -> SceneDesc:
     return s
 
 
+def textured_box(seed: int = 12) -> SceneDesc:
+    """Cornell box whose back, left and right walls and floor carry TexR albedo (PNG, PPM, BMP
+    and PFM images), with uvs tiled 3x and shifted negative so that the fract wrap matters,
+    plus a glossy box with a textured G.R (rt.hpp:1947-1979)."""
+    rng = np.random.default_rng(seed)
+    s = cornell_box()
+    names = {"back": "back.png", "left": "left.ppm", "right": "right.bmp", "floor": "floor.pfm"}
+    for name, fn in names.items():
+        hh, ww = int(rng.integers(3, 9)), int(rng.integers(3, 9))
+        img = rng.integers(10, 240, (hh, ww, 3)).astype(np.float32) / np.float32(255.0)
+        if fn.endswith(".pfm"):
+            img = rng.uniform(0.05, 0.9, (hh, ww, 3)).astype(np.float32)
+        s.textures[fn] = img
+        for p in s.primitives:
+            if p.name == name:
+                p.params = {"D": {"TexR": fn}}
+                p.mesh.uvs = _f32(p.mesh.uvs.astype(np.float64) * 3.0 - 1.3)
+    s.textures["gloss.png"] = rng.integers(30, 230, (4, 5, 3)).astype(np.float32) / np.float32(255.0)
+    for p in s.primitives:
+        if p.name == "shortbox":
+            p.type = ["G"]
+            p.params = {"G": {"TexR": "gloss.png", "Eta": list(GOLD_ETA), "K": list(GOLD_K),
+                              "Roughness": phong_to_beckmann(50.0)}}
+            n = len(p.mesh.positions)
+            p.mesh.uvs = _f32(np.stack([np.arange(n) % 4 / 4.0 + 0.1, np.arange(n) // 4 % 4 / 4.0 + 0.1], 1))
+    return s
+
+
 def sphere_field(num_spheres=40, grid=96, level=3, seed=11) -> SceneDesc:
     """A small terrain_scene (same generator, fewer triangles) for traversal tests."""
     s = terrain_scene(num_spheres=num_spheres, grid=grid, level=level, seed_terrain=seed, seed_spheres=seed + 1)
     return s
 
 
-WORKLOADS.update({"material_box": material_box, "area_sensor_box": area_sensor_box, "sphere_field": sphere_field})
+WORKLOADS.update({"material_box": material_box, "area_sensor_box": area_sensor_box, "sphere_field": sphere_field,
+                  "textured_box": textured_box})
 
 
 def inverse_box(seed: int = 5, emitter_seed: int = 7) -> SceneDesc:

@@ -130,7 +130,22 @@ struct Prim {
     dv3 eye, Vx, Vy, Vz, We;
     double fov = 0, aspect = 1;
     dv3 DR, GR, Geta, Gk, SR;
+    std::vector<float> Dtex, Gtex;  // TexR texels (copies of the descriptor's arrays)
 };
+
+void CopyTextures(Prim& p) {
+    if (p.d.D_tex) p.Dtex.assign(p.d.D_tex, p.d.D_tex + 3 * (size_t)p.d.D_tex_w * p.d.D_tex_h);
+    if (p.d.G_tex) p.Gtex.assign(p.d.G_tex, p.d.G_tex + 3 * (size_t)p.d.G_tex_w * p.d.G_tex_h);
+    p.d.D_tex = p.d.G_tex = nullptr;
+}
+
+// Texture::Evaluate (rt.hpp:260-266): nearest texel, uv wrapped by fract.
+dv3 TexEval(const std::vector<float>& tex, int w, int h, const double uv[2]) {
+    const int x = std::min(std::max((int)((uv[0] - std::floor(uv[0])) * w), 0), w - 1);
+    const int y = std::min(std::max((int)((uv[1] - std::floor(uv[1])) * h), 0), h - 1);
+    const size_t i = (size_t)w * y + x;
+    return dv3(tex[3 * i], tex[3 * i + 1], tex[3 * i + 2]);
+}
 
 dv3 V(const double a[3]) { return {a[0], a[1], a[2]}; }
 
@@ -680,7 +695,8 @@ dv3 EvaluateDirection(const Prim& p, const Geom& g, int type, dv3 wi, dv3 wo, bo
     }
     if (type & D) {
         if (lwi.z <= 0 || lwo.z <= 0) return zero;
-        return p.DR * InvPi * corr;
+        const dv3 R = p.Dtex.empty() ? p.DR : TexEval(p.Dtex, p.d.D_tex_w, p.d.D_tex_h, g.uv);
+        return R * InvPi * corr;
     }
     if (type & G) {
         if (lwi.z <= 0 || lwo.z <= 0) return zero;
@@ -688,7 +704,8 @@ dv3 EvaluateDirection(const Prim& p, const Geom& g, int type, dv3 wi, dv3 wo, bo
         const double Dd = Beckmann(p, H);
         const double Gg = ShadowMasking(lwi, lwo, H);
         const dv3 F = FrConductor(p, dot(lwi, H));
-        return p.GR * Dd * Gg * F / (4.0 * lwi.z) / lwo.z * corr;
+        const dv3 R = p.Gtex.empty() ? p.GR : TexEval(p.Gtex, p.d.G_tex_w, p.d.G_tex_h, g.uv);
+        return R * Dd * Gg * F / (4.0 * lwi.z) / lwo.z * corr;
     }
     if (type & S) {
         if (!force) return zero;
@@ -1059,6 +1076,7 @@ ora_scene* Build(const ora_prim_desc* prims, int n_prims, const float* tri_pos, 
         p.ldir = V(p.d.l_direction);
         p.DR = V(p.d.D_R);
         p.GR = V(p.d.G_R);
+        CopyTextures(p);
         p.Geta = V(p.d.G_eta);
         p.Gk = V(p.d.G_k);
         p.SR = V(p.d.S_R);
@@ -1235,6 +1253,7 @@ static Prim HookPrim(const ora_prim_desc* d) {
     p.Geta = V(d->G_eta);
     p.Gk = V(d->G_k);
     p.SR = V(d->S_R);
+    CopyTextures(p);
     return p;
 }
 static Geom HookGeom() {

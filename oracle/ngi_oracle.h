@@ -41,6 +41,12 @@ typedef struct ora_prim_desc {
     int32_t has_uv;
     double S_R[3];
     double S_eta1, S_eta2;
+    /* TexR images (rt.hpp:157-270): rgb floats, row 0 = the image's top row; NULL = constant R.
+     * Copied by ora_scene_create. */
+    const float* D_tex;
+    int32_t D_tex_w, D_tex_h;
+    const float* G_tex;
+    int32_t G_tex_w, G_tex_h;
 } ora_prim_desc;
 
 typedef struct ora_render_params {

@@ -45,6 +45,8 @@ class PrimDesc(ctypes.Structure):
         ("G_roughness", ctypes.c_double),
         ("s_type", ctypes.c_int32), ("has_uv", ctypes.c_int32),
         ("S_R", ctypes.c_double * 3), ("S_eta1", ctypes.c_double), ("S_eta2", ctypes.c_double),
+        ("D_tex", ctypes.c_void_p), ("D_tex_w", ctypes.c_int32), ("D_tex_h", ctypes.c_int32),
+        ("G_tex", ctypes.c_void_p), ("G_tex_w", ctypes.c_int32), ("G_tex_h", ctypes.c_int32),
     ]
 
 
@@ -98,9 +100,17 @@ def _p(a: np.ndarray):
 TYPE_BITS = {"D": 1, "G": 2, "S": 4, "L": 8, "E": 16}
 
 
-def prim_desc(type_list, params: dict) -> PrimDesc:
-    """PrimDesc from the schema's type list and params mapping (schema.yml:33-334)."""
+def prim_desc(type_list, params: dict, textures=None, keep=None) -> PrimDesc:
+    """PrimDesc from the schema's type list and params mapping (schema.yml:33-334).
+    `textures` maps a TexR path to its texels ((H, W, 3) float32, row 0 = the image's top
+    row); the arrays handed to the oracle are appended to `keep`."""
     d = PrimDesc()
+
+    def tex(name):
+        a = np.ascontiguousarray(np.asarray(textures[name], np.float32))
+        keep.append(a)
+        return a.ctypes.data, a.shape[1], a.shape[0]
+
     for t in type_list:
         d.type |= TYPE_BITS[t]
 
@@ -127,10 +137,16 @@ def prim_desc(type_list, params: dict) -> PrimDesc:
             d.up = v3(E["pinhole"]["view"]["up"])
             d.fov_deg = float(E["pinhole"]["perspective"]["fov"])
     if "D" in params and (d.type & 1):
-        d.D_R = v3(params["D"]["R"])
+        if "R" in params["D"]:
+            d.D_R = v3(params["D"]["R"])
+        else:
+            d.D_tex, d.D_tex_w, d.D_tex_h = tex(params["D"]["TexR"])
     if "G" in params and (d.type & 2):
         G = params["G"]
-        d.G_R = v3(G["R"])
+        if "R" in G:
+            d.G_R = v3(G["R"])
+        else:
+            d.G_tex, d.G_tex_w, d.G_tex_h = tex(G["TexR"])
         d.G_eta = v3(G["Eta"])
         d.G_k = v3(G["K"])
         d.G_roughness = float(G["Roughness"])
@@ -145,13 +161,14 @@ def prim_desc(type_list, params: dict) -> PrimDesc:
     return d
 
 
-def flatten(primitives):
+def flatten(primitives, textures=None, keep=None):
     """primitives: iterable of (type_list, params, mesh-or-None) where mesh has positions,
     normals, faces, uvs. Returns (PrimDesc array, tri_pos, tri_nrm, tri_uv)."""
     descs, pos, nrm, uvs = [], [], [], []
+    keep = [] if keep is None else keep
     first = 0
     for type_list, params, mesh in primitives:
-        d = prim_desc(type_list, params)
+        d = prim_desc(type_list, params, textures, keep)
         if mesh is not None:
             F = np.asarray(mesh.faces, np.int64)
             P = np.asarray(mesh.positions, np.float32)
@@ -174,8 +191,9 @@ def flatten(primitives):
 
 
 class OracleScene:
-    def __init__(self, primitives, aspect: float):
-        self.descs, self.pos, self.nrm, self.uv = flatten(primitives)
+    def __init__(self, primitives, aspect: float, textures=None):
+        self._tex_keep = []
+        self.descs, self.pos, self.nrm, self.uv = flatten(primitives, textures, self._tex_keep)
         h = lib().ora_scene_create(self.descs, len(self.descs), _p(self.pos), _p(self.nrm), _p(self.uv),
                                    len(self.pos), float(aspect))
         if not h:
@@ -184,7 +202,7 @@ class OracleScene:
 
     @classmethod
     def from_desc(cls, desc, aspect: float) -> "OracleScene":
-        return cls([(p.type, p.params, p.mesh) for p in desc.primitives], aspect)
+        return cls([(p.type, p.params, p.mesh) for p in desc.primitives], aspect, getattr(desc, "textures", None))
 
     def close(self):
         if self._h:

@@ -153,3 +153,93 @@ def test_cli_usage_and_errors(native_lib, tmp_path):
     assert r.returncode != 0 and "ERROR" in r.stderr
     r = subprocess.run([str(cli), "-n"], capture_output=True, text=True)
     assert r.returncode != 0
+
+
+def _film(w, h, seed=0):
+    rng = np.random.default_rng(seed)
+    f = rng.lognormal(-1.0, 1.5, (h, w, 3))
+    f[0, 0] = (0.0, -1.0, np.nan)  # black, negative, NaN
+    f[-1, -1] = (1e6, 1.0, 0.5)
+    return np.ascontiguousarray(f)
+
+
+def test_exr_writer_layout(native_lib, tmp_path):
+    """Scanline OpenEXR 2.0: header attributes, offset table, float B/G/R planes, top row = film
+    row H-1 (the reference flips y before tinyexr, basic.hpp:586-592)."""
+    import struct
+
+    import nanogi_gb300 as ng
+
+    w, h = 7, 5
+    film = _film(w, h)
+    path = tmp_path / "deep" / "dir" / "f.exr"  # the directory is created, as the reference does
+    ng.save_image(path, film)
+    b = path.read_bytes()
+    assert b[:4] == bytes([0x76, 0x2F, 0x31, 0x01]) and struct.unpack("<I", b[4:8])[0] == 2
+    pos, attrs = 8, {}
+    while b[pos] != 0:
+        name_end = b.index(b"\0", pos)
+        type_end = b.index(b"\0", name_end + 1)
+        name, typ = b[pos:name_end].decode(), b[name_end + 1:type_end].decode()
+        size = struct.unpack("<i", b[type_end + 1:type_end + 5])[0]
+        attrs[name] = (typ, b[type_end + 5:type_end + 5 + size])
+        pos = type_end + 5 + size
+    pos += 1
+    assert attrs["compression"] == ("compression", b"\0")
+    assert struct.unpack("<4i", attrs["dataWindow"][1]) == (0, 0, w - 1, h - 1)
+    ch = attrs["channels"][1]
+    names = []
+    q = 0
+    while ch[q] != 0:
+        e = ch.index(b"\0", q)
+        names.append(ch[q:e].decode())
+        assert struct.unpack("<i", ch[e + 1:e + 5])[0] == 2  # FLOAT
+        q = e + 17
+    assert names == ["B", "G", "R"]
+    offsets = struct.unpack(f"<{h}Q", b[pos:pos + 8 * h])
+    for y, off in enumerate(offsets):
+        yy, size = struct.unpack("<ii", b[off:off + 8])
+        assert yy == y and size == 12 * w
+        planes = np.frombuffer(b[off + 8:off + 8 + size], "<f4").reshape(3, w)
+        expect = film[h - 1 - y].astype(np.float32)
+        got = np.stack([planes[2], planes[1], planes[0]], 1)
+        assert np.array_equal(got, expect, equal_nan=True)
+
+
+def test_png_writer_tone_map(native_lib, tmp_path):
+    """8-bit RGB PNG with the reference's tone map clamp(int(255 v^(1/2.2)), 0, 255)
+    (basic.hpp:625-634), top row = film row H-1; decoded with zlib and checked by CRC."""
+    import struct
+    import zlib
+
+    import nanogi_gb300 as ng
+
+    w, h = 9, 4
+    film = _film(w, h, seed=3)
+    path = tmp_path / "f.png"
+    ng.save_image(path, film)
+    b = path.read_bytes()
+    assert b[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, chunks = 8, {}
+    while pos < len(b):
+        n = struct.unpack(">I", b[pos:pos + 4])[0]
+        typ, data = b[pos + 4:pos + 8], b[pos + 8:pos + 8 + n]
+        assert struct.unpack(">I", b[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(typ + data)
+        chunks[typ] = chunks.get(typ, b"") + data
+        pos += 12 + n
+    assert struct.unpack(">IIBBBBB", chunks[b"IHDR"]) == (w, h, 8, 2, 0, 0, 0)
+    raw = np.frombuffer(zlib.decompress(chunks[b"IDAT"]), np.uint8).reshape(h, 1 + 3 * w)
+    assert not raw[:, 0].any()
+    img = raw[:, 1:].reshape(h, w, 3)
+    with np.errstate(invalid="ignore"):
+        v = np.power(film[::-1], 1 / 2.2) * 255.0
+    expect = np.where(np.isnan(v), 0, np.clip(np.where(v >= 255, 255, np.trunc(np.nan_to_num(v, nan=0))), 0, 255))
+    assert np.array_equal(img, expect.astype(np.uint8))
+
+
+def test_save_image_rejects_unknown_extensions(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+
+    with pytest.raises(ng.NanogiError) as e:
+        ng.save_image(tmp_path / "f.jpg", np.zeros((2, 2, 3)))
+    assert "Invalid extension" in e.value.message

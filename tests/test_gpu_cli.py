@@ -1,0 +1,43 @@
+"""The nanogi command line on the GPU: renderer names, the time budget and progress images
+(src/nanogi.cpp:356-404, 2000-2023)."""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.mark.parametrize("renderer,ext", [("pt", ".hdr"), ("ptdirect", ".exr"), ("ltdirect", ".png")])
+def test_cli_renders_every_format(native_lib, cornell, tmp_path, renderer, ext):
+    _, path = cornell
+    out = tmp_path / "out" / f"img{ext}"
+    cli = ROOT / "nanogi_gb300" / "_build" / "nanogi"
+    r = subprocess.run([str(cli), renderer, str(path), str(out), "16", "12", "-n", "20000", "-m", "6", "--seed", "3"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert out.stat().st_size > 0
+
+
+def test_cli_time_budget_writes_progress_images(native_lib, cornell, tmp_path):
+    import nanogi_gb300 as ng
+
+    _, path = cornell
+    cli = ROOT / "nanogi_gb300" / "_build" / "nanogi"
+    fmt = str(tmp_path / "progress" / "{{count}}.hdr")
+    out = tmp_path / "final.hdr"
+    r = subprocess.run([str(cli), "ptdirect", str(path), str(out), "32", "32", "-t", "1.0", "-m", "6",
+                        "--progress-image-update-interval", "0.2", "--progress-image-update-format", fmt],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    images = sorted((tmp_path / "progress").glob("*.hdr"))
+    assert len(images) >= 2
+    assert images[0].name == "0000000001.hdr"
+    last = ng.load_hdr(images[-1], 32, 32)
+    final = ng.load_hdr(out, 32, 32)
+    assert last.mean() > 0 and abs(last.mean() / final.mean() - 1) < 0.2

@@ -142,7 +142,7 @@ scene:
     ("version: 5\nscene:\n  primitives:\n    - type: [D]\n      mesh:\n        path: missing.obj\n"
      "      params:\n        D:\n          R: [1, 1, 1]\n", "NGI_ERR_IO"),
     ("version: 5\nscene:\n  primitives:\n    - type: [D]\n      mesh:\n        path: quad.obj\n"
-     "      params:\n        D:\n          TexR: tex.png\n", "NGI_ERR_UNSUPPORTED"),
+     "      params:\n        D:\n          TexR: missing.png\n", "NGI_ERR_IO"),
     ("version: 5\nscene:\n  primitives:\n    - type: [D]\n      mesh:\n        path: quad.obj\n"
      "      params:\n        D:\n          R: [1, 1]\n", "NGI_ERR_PARSE"),
     ("version: 5\nscene:\n  primitives:\n    - type: [D\n", "NGI_ERR_PARSE"),
@@ -232,3 +232,65 @@ def test_memory_mesh_flat_normals_and_errors(native_lib, tmp_path):
     del mm[k0]
     with pytest.raises(ng.NanogiError):
         ng.Scene.load_with_meshes(path, 1.0, mm)
+
+
+@pytest.mark.parametrize("ext", [".png", ".ppm", ".bmp", ".pfm"])
+def test_texture_decoders_round_trip(native_lib, tmp_path, ext):
+    """TexR images decode to the texels they were written from (8-bit as v/255), top row first."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    rng = np.random.default_rng(len(ext))
+    img = (rng.integers(0, 256, (13, 17, 3)) / np.float32(255.0)).astype(np.float32)
+    if ext == ".pfm":
+        img = rng.uniform(-1, 4, (13, 17, 3)).astype(np.float32)
+    path = tmp_path / f"t{ext}"
+    scenegen.write_texture(path, img)
+    got = ng.load_texture(path)
+    assert got.shape == img.shape
+    assert np.array_equal(got, img)
+
+
+def test_png_decoder_handles_rgba_stored_blocks_and_bad_files(native_lib, tmp_path):
+    import struct
+    import zlib
+
+    import nanogi_gb300 as ng
+
+    def png(w, h, ctype, raw, level=9, depth=8):
+        def chunk(t, d):
+            return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d))
+        return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+                + chunk(b"IDAT", zlib.compress(raw, level)) + chunk(b"IEND", b""))
+
+    rng = np.random.default_rng(5)
+    rgba = rng.integers(0, 256, (6, 4, 4), dtype=np.uint8)
+    raw = b"".join(b"\x00" + rgba[y].tobytes() for y in range(6))
+    for level in (0, 1, 9):  # stored, fixed and dynamic Huffman blocks
+        p = tmp_path / f"a{level}.png"
+        p.write_bytes(png(4, 6, 6, raw, level))
+        got = ng.load_texture(p)
+        assert np.array_equal(got, rgba[:, :, :3].astype(np.float32) / np.float32(255.0))
+    gray = tmp_path / "g.png"
+    gray.write_bytes(png(4, 6, 0, b"".join(b"\x00" + bytes(4) for _ in range(6))))
+    with pytest.raises(ng.NanogiError) as e:
+        ng.load_texture(gray)
+    assert e.value.status == 7  # the reference accepts 24/32-bit bitmaps only
+    bad = tmp_path / "bad.png"
+    bad.write_bytes(png(4, 6, 2, b"\x00" * 10))
+    with pytest.raises(ng.NanogiError):
+        ng.load_texture(bad)
+    with pytest.raises(ng.NanogiError):
+        ng.load_texture(tmp_path / "missing.png")
+
+
+def test_textured_scene_loads(native_lib, tmp_path):
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    desc = scenegen.textured_box()
+    s = ng.Scene.load(scenegen.write_scene(desc, tmp_path), 1.0)
+    assert s.info()["num_primitives"] == len(desc.primitives)
+    (tmp_path / "left.ppm").unlink()
+    with pytest.raises(ng.NanogiError):
+        ng.Scene.load(tmp_path / "scene.yml", 1.0)

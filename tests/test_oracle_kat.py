@@ -267,3 +267,28 @@ def test_ltdirect_keeps_the_reference_position_pdf(oracle_lib):
     pt = o.render("ptdirect", seed=1, **kw)
     ltd = o.render("ltdirect", seed=2, **kw)
     assert ltd.sum() / pt.sum() == pytest.approx(0.0625, rel=0.02)
+
+
+def test_constant_textures_render_like_constant_albedo(oracle_lib):
+    """TexR lookups (rt.hpp:260-266): a texture whose texels all equal R renders exactly like R."""
+    import copy
+
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    plain = scenegen.cornell_box()
+    for p in plain.primitives:  # albedos a float texel holds exactly
+        if p.type == ["D"]:
+            p.params["D"]["R"] = [float(np.float32(x)) for x in p.params["D"]["R"]]
+    tex = copy.deepcopy(plain)
+    for i, p in enumerate(tex.primitives):
+        if p.type == ["D"]:
+            name = f"t{i}.pfm"
+            tex.textures[name] = np.broadcast_to(np.float32(p.params["D"]["R"]), (3, 5, 3)).copy()
+            p.params = {"D": {"TexR": name}}
+            p.mesh.uvs = scenegen._f32(np.random.default_rng(i).uniform(-3, 3, (len(p.mesh.positions), 2)))
+    kw = dict(num_samples=16 * 16 * 16, max_vertices=6, width=16, height=16, seed=2, threads=1)
+    for r in ("pt", "ptdirect", "ltdirect"):
+        a = OracleScene.from_desc(plain, 1.0).render(r, **kw)
+        b = OracleScene.from_desc(tex, 1.0).render(r, **kw)
+        assert np.array_equal(a, b), r  # one thread: the same summation order
