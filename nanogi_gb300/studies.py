@@ -1,6 +1,6 @@
 """Measurement studies beyond the throughput line of bench.py.
 
-    python -m nanogi_gb300.studies convergence [--ref-spp 8192]
+    python -m nanogi_gb300.studies convergence [--ref-spp 65536]
     python -m nanogi_gb300.studies adjoint
     python -m nanogi_gb300.studies batch
     python -m nanogi_gb300.studies precision [--ref-spp 1024]
@@ -49,7 +49,7 @@ def _render(ng, scene, renderer, precision, spp, w, h, m, seed, offset=0):
     return film, r.last_stats["render_ms"] / 1e3, wall
 
 
-def convergence(ref_spp: int = 8192, w: int = 256, h: int = 256, m: int = 8, max_ladder_spp: int = 4096):
+def convergence(ref_spp: int = 65536, w: int = 256, h: int = 256, m: int = 8, max_ladder_spp: int = 4096):
     import nanogi_gb300 as ng
     from nanogi_gb300 import scenegen
 
@@ -286,17 +286,17 @@ def main():
     ap.add_argument("study", choices=["convergence", "adjoint", "batch", "precision"])
     ap.add_argument("--triangles", type=int, default=10_000_000)
     ap.add_argument("--res", type=int, default=1024)
-    ap.add_argument("--ref-spp", type=int, default=8192)
+    ap.add_argument("--ref-spp", type=int, default=None)
     ap.add_argument("--max-ladder-spp", type=int, default=4096)
     a = ap.parse_args()
     if a.study == "convergence":
-        print(json.dumps(convergence(a.ref_spp, max_ladder_spp=a.max_ladder_spp)), flush=True)
+        print(json.dumps(convergence(a.ref_spp or 65536, max_ladder_spp=a.max_ladder_spp)), flush=True)
     elif a.study == "adjoint":
         print(json.dumps(adjoint_cost()), flush=True)
     elif a.study == "batch":
         print(json.dumps(batch()), flush=True)
     elif a.study == "precision":
-        print(json.dumps(precision(a.ref_spp, a.res, a.res, num_triangles=a.triangles)), flush=True)
+        print(json.dumps(precision(a.ref_spp or 1024, a.res, a.res, num_triangles=a.triangles)), flush=True)
 
 
 if __name__ == "__main__":
