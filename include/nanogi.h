@@ -52,7 +52,9 @@ typedef enum ngi_renderer_type {
     NGI_RENDERER_PT = 0,       /* "pt"       : ProcessSample_PT       src/nanogi.cpp:446-607 */
     NGI_RENDERER_PTDIRECT = 1, /* "ptdirect" : ProcessSample_PTDirect src/nanogi.cpp:609-802 */
     NGI_RENDERER_LT = 2,       /* "lt"       : ProcessSample_LT       src/nanogi.cpp:804-955 */
-    NGI_RENDERER_LTDIRECT = 3  /* "ltdirect" : ProcessSample_LTDirect src/nanogi.cpp:957-1131 */
+    NGI_RENDERER_LTDIRECT = 3, /* "ltdirect" : ProcessSample_LTDirect src/nanogi.cpp:957-1131 */
+    NGI_RENDERER_BDPT = 4      /* "bdpt"     : ProcessSample_BDPT     src/nanogi.cpp:1133-1194, include/nanogi/bdpt.hpp;
+                                  subpaths keep at most 32 vertices */
 } ngi_renderer_type;
 
 /* Arithmetic of the shading stage. Traversal is FP32 and accumulation FP64 in both. */

@@ -23,7 +23,7 @@ STATUS_NAMES = {
     7: "NGI_ERR_UNSUPPORTED",
     8: "NGI_ERR_NO_DEVICE",
 }
-RENDERERS = {"pt": 0, "ptdirect": 1, "lt": 2, "ltdirect": 3}
+RENDERERS = {"pt": 0, "ptdirect": 1, "lt": 2, "ltdirect": 3, "bdpt": 4}
 PRECISIONS = {"fp32": 0, "fp64": 1}
 RASTER_MODES = {"stratified": 0, "uniform": 1}
 RAY_OFFSETS = {"reference": 0, "scaled": 1}

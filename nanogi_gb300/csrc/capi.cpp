@@ -55,8 +55,8 @@ ngi_status Guard(F&& f) {
 ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
     if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
     if (!p) return Fail(NGI_ERR_INVALID_ARGUMENT, "params is NULL");
-    if (p->renderer < NGI_RENDERER_PT || p->renderer > NGI_RENDERER_LTDIRECT)
-        return Fail(NGI_ERR_INVALID_ARGUMENT, "renderer must be pt, ptdirect, lt or ltdirect");
+    if (p->renderer < NGI_RENDERER_PT || p->renderer > NGI_RENDERER_BDPT)
+        return Fail(NGI_ERR_INVALID_ARGUMENT, "renderer must be pt, ptdirect, lt, ltdirect or bdpt");
     if (p->width <= 0 || p->height <= 0) return Fail(NGI_ERR_INVALID_ARGUMENT, "width and height must be positive");
     if ((int64_t)p->width * (int64_t)p->height > ((int64_t)1 << 31) - 1)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "width*height must fit in 31 bits");

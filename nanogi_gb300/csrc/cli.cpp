@@ -140,8 +140,10 @@ int main(int argc, char** argv) {
     else if (r == "ptdirect") p.renderer = NGI_RENDERER_PTDIRECT;
     else if (r == "lt") p.renderer = NGI_RENDERER_LT;
     else if (r == "ltdirect") p.renderer = NGI_RENDERER_LTDIRECT;
+    else if (r == "bdpt") p.renderer = NGI_RENDERER_BDPT;
     else {
-        std::fprintf(stderr, "ERROR : renderer '%s' is not built (available: pt, ptdirect, lt, ltdirect)\n", r.c_str());
+        std::fprintf(stderr, "ERROR : renderer '%s' is not built (available: pt, ptdirect, lt, ltdirect, bdpt)\n",
+                     r.c_str());
         return EXIT_FAILURE;
     }
     try {

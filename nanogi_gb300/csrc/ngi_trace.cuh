@@ -82,6 +82,16 @@ constexpr int kTraversalStack = 64;
 // ulps of rounding in the slab distances (Ize, JCGT 2013).
 constexpr float kBoxLo = 1.0f - 1.0f / 1048576.0f;
 constexpr float kBoxHi = 1.0f + 1.0f / 1048576.0f;
+// tn Lo <= tf Hi as one product, tn <= tf (Hi / Lo): the same test for either sign of tn and tf.
+constexpr float kBoxRatio = kBoxHi / kBoxLo;
+#ifndef NGI_BOX_ONEMUL
+#define NGI_BOX_ONEMUL 1
+#endif
+// Node phase "while-while" (Aila and Laine 2009): a lane holding triangles waits while the
+// other lanes of its warp keep visiting nodes, so the triangle tests of a warp run together.
+#ifndef NGI_WHILE_WHILE
+#define NGI_WHILE_WHILE 1
+#endif
 
 struct TraceStats {
     uint32_t nodes;
@@ -215,7 +225,11 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 #endif
             const float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
             const float tf = fminf(fminf(x1, y1), fminf(z1, s.tmax));
+#if NGI_BOX_ONEMUL
+            if (m != 0u && tn <= tf * kBoxRatio) {
+#else
             if (m != 0u && tn * kBoxLo <= tf * kBoxHi) {
+#endif
                 const uint32_t child_bits = m >> 5;
                 const bool inner = (m & 0x18u) == 0x18u;
                 const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ s.octinv) : (m & 0x1Fu);
@@ -236,6 +250,63 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 template <bool ANY_HIT, bool STATS>
 NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
                      bool& stack_overflow, TraceStats* stats, int postpone_pct) {
+#if NGI_WHILE_WHILE
+    if (postpone_pct <= 0) {
+        // node phase: every lane without triangles visits nodes until all lanes hold triangles or
+        // have run out of nodes
+        const unsigned act = __activemask();
+        uint2 tg = make_uint2(0u, 0u);
+        while (true) {
+            const bool want = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
+            if (!__any_sync(act, want)) break;
+            if (want) {
+                const uint32_t hits = s.ngroup.y;
+                const int bit = 31 - __clz(hits);
+                s.ngroup.y &= ~(1u << bit);
+                if (s.ngroup.y > 0x00FFFFFFu) {
+                    if (s.sp == kTraversalStack) {
+                        stack_overflow = true;
+                        s.hit = -1;
+                        s.ngroup = make_uint2(0u, 0u);
+                        s.sp = 0;
+                        continue;
+                    }
+                    stack[s.sp++] = s.ngroup;
+                }
+                const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
+                const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+                const uint32_t node = s.ngroup.x + rel;
+                uint32_t child_base, tri_base, imask;
+                const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
+                if (STATS) stats->nodes++;
+                s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
+                tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
+                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
+            }
+        }
+        while (tg.y != 0u) {
+            const int tb = 31 - __clz(tg.y);
+            tg.y &= ~(1u << tb);
+            const uint32_t ti = tg.x + (uint32_t)tb;
+            const float4* tp = tris + 3 * (size_t)ti;
+            const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            if (STATS) stats->tris++;
+            float t, u, v;
+            if (tri_intersect(s.rp, p0, p1, p2, s.tmin, s.tmax, t, u, v)) {
+                s.tmax = t;
+                s.hu = u;
+                s.hv = v;
+                s.hit = (int)ti;
+                if (ANY_HIT) return true;
+            }
+        }
+        if (s.ngroup.y <= 0x00FFFFFFu) {
+            if (s.sp == 0) return true;
+            s.ngroup = stack[--s.sp];
+        }
+        return false;
+    }
+#endif
     uint2 tgroup;
     if (s.ngroup.y > 0x00FFFFFFu) {
         const uint32_t hits = s.ngroup.y;

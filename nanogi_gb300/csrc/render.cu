@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "device_scene.hpp"
+#include "ngi_bdpt.cuh"
 #include "ngi_shade.cuh"
 #include "ngi_trace.cuh"
 #include "scene.hpp"
@@ -114,6 +115,9 @@ struct WaveView {
     // batches only (null otherwise)
     int* job;                // per slot: job of the path
     int* sh_job;             // per shadow ray: job of the ray
+    // bdpt only (null otherwise)
+    BdVert<R>* bd_verts;     // per slot: light subpath then eye subpath, kBdptMaxVertices each
+    int4* bd_info;           // per slot: phase | pending << 8, #light vertices, #eye vertices, cursor n << 8 | s
 };
 
 // Longest surface-vertex prefix the adjoint carries: paths of up to 17 vertices.
@@ -123,6 +127,7 @@ struct RenderWave {
     int Q = 0;
     int precision = -1;
     bool adjoint_buffers = false;
+    int bdpt_precision = -1;  // precision the bdpt vertex arrays were sized for
     std::vector<void*> bufs;
     WaveCounters* ctr = nullptr;
     WaveCounters* h_ctr = nullptr;   // pinned
@@ -889,6 +894,249 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
     }
 }
 
+// ---- bdpt (ProcessSample_BDPT, src/nanogi.cpp:1133-1194) ---------------------------------------
+// Leaves vertex V[nv-1] of a subpath (Path::SampleSubpath, bdpt.hpp:86-104): samples the next
+// direction with the vertex's own sampling routine and queues the extension ray, or returns
+// false where the subpath ends (length limit or a zero f). Random numbers: vertex j leaves with
+// (vbase + j + 2, RNG_DIR).
+template <typename R>
+NGI_D bool bd_extend(const SceneView<R>& sv, const RenderConsts& rc, const WaveView<R>& w, int s, const BdVert<R>* V,
+                     int nv, uint32_t vbase, const RngKey& rk, bool le) {
+    if ((rc.max_vertices != -1 && nv >= rc.max_vertices) || nv >= kBdptMaxVertices) return false;
+    const int j = nv - 1;
+    const BdVert<R>& v = V[j];
+    const Geom<R> g = bd_geom(v);
+    const V3<R> wi = j >= 1 ? bd_dir(v, V[j - 1]) : v3<R>(0, 0, 0);
+    const float4 ud = rng4(rk, vbase + (uint32_t)j + 2u, RNG_DIR);
+    const DevMaterial<R>& m = sv.mats[v.prim];
+    V3<R> wo;
+    if (v.type & DT_L) {
+        V3<R> wgt;
+        if (!light_sample_direction(sv.lights[m.light_index], g, (R)ud.x, (R)ud.y, wo, wgt)) return false;
+    } else if (v.type & DT_E) {
+        const DevSensor<R>& cam = sv.sensor;
+        if (cam.type == ET_PINHOLE) {
+            wo = pinhole_direction(cam, (R)ud.x, (R)ud.y);
+            if (pinhole_importance(cam, wo) == R(0)) return false;
+        } else {
+            wo = to_world(g, cosine_hemisphere((R)ud.x, (R)ud.y));
+            if (!(to_local(g, wo).z > R(0)) || is_zero(cam.We)) return false;
+        }
+    } else {
+        if (!bsdf_sample(m, g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo)) return false;
+        if (is_zero(bsdf_eval(m, material_albedo(sv, m, g), g, wi, wo, true, le))) return false;
+    }
+    store_ray(w, s, g, wo, rc.ray_offset);
+    return true;
+}
+
+// Vertex 0 of a subpath (bdpt.hpp:62-78): a light chosen uniformly (light subpath) or the
+// sensor, and a position on it, from (vbase + 1, RNG_SENSOR): .z the choice, .xy the position.
+template <typename R>
+NGI_D void bd_first_vertex(const SceneView<R>& sv, BdVert<R>* V, uint32_t vbase, const RngKey& rk, bool light) {
+    const float4 u = rng4(rk, vbase + 1u, RNG_SENSOR);
+    Geom<R> g;
+    if (light) {
+        const int nl = sv.num_lights;
+        int li = (int)((R)u.z * (R)nl);
+        li = li < 0 ? 0 : (li > nl - 1 ? nl - 1 : li);
+        const DevLight<R>& L = sv.lights[li];
+        sample_light_position(sv, L, (R)u.x, (R)u.y, g);
+        V[0] = bd_vert(g, L.prim, DT_L);
+    } else {
+        const DevSensor<R>& cam = sv.sensor;
+        if (cam.type == ET_PINHOLE) {
+            g.p = cam.eye;
+            g.degenerated = true;
+            g.ext = 0.0f;
+            g.sn = g.gn = g.du = g.dv = v3<R>(0, 0, 0);
+            g.uvx = g.uvy = R(0);
+        } else {
+            sample_mesh_position(sv, cam.tri_base, cam.tri_count, cam.cdf_offset, (R)u.x, (R)u.y, g);
+        }
+        V[0] = bd_vert(g, cam.prim, DT_E);
+    }
+}
+
+// Evaluates strategies (n, s) of a sample from the cursor on (Path::Connect and
+// EvaluateContribution / SelectionProb, bdpt.hpp:133-211): strategies without a connection
+// (s = 0 or t = 0) go to the film, the others become at most two shadow rays. Returns true
+// when every strategy is done; otherwise `cursor` holds the next one.
+template <typename R>
+NGI_D bool bd_connect(const SceneView<R>& sv, const RenderConsts& rc, const WaveView<R>& w, const BdVert<R>* VL,
+                      const BdVert<R>* VE, int nL, int nE, int& cursor, ShadowRay<R>* out) {
+    int emitted = 0;
+    int n = cursor >> 8, s0 = cursor & 0xFF;
+    for (; n <= nL + nE; n++, s0 = -1) {
+        if (rc.max_vertices != -1 && n > rc.max_vertices) continue;
+        const int smin = n - nE > 0 ? n - nE : 0, smax = nL < n ? nL : n;
+        for (int s = s0 > smin ? s0 : smin; s <= smax; s++) {
+            if (emitted == 2) {
+                cursor = (n << 8) | s;
+                return false;
+            }
+            const int t = n - s;
+            if (s == 0 && !(sv.mats[VE[t - 1].prim].type & DT_L)) continue;
+            if (t == 0 && !(sv.mats[VL[s - 1].prim].type & DT_E)) continue;
+            BdPath<R> x;
+            x.L = VL;
+            x.E = VE;
+            x.s = s;
+            x.n = n;
+            V3<R> C = bd_unweighted(sv, x);
+            if (is_zero(C)) continue;
+            C = C * bd_mis_weight(sv, x) / bd_selection_prob<R>(n, s);
+            if (is_zero(C)) continue;
+            if (!finite3(C)) {
+                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                continue;
+            }
+            // Path::RasterPosition (bdpt.hpp:204-211)
+            const BdVert<R>& v = x.at(n - 1);
+            R rx = R(0), ry = R(0);
+            if (sv.mats[v.prim].e_type == ET_PINHOLE) pinhole_raster(sv.sensor, bd_dir(v, x.at(n - 2)), rx, ry);
+            else { rx = v.uvx; ry = v.uvy; }
+            const uint32_t pixel = (uint32_t)pixel_index(rx, ry, rc.width, rc.height);
+            if (s > 0 && t > 0) {
+                ShadowRay<R>& o = out[emitted++];
+                shadow_segment(bd_geom(VL[s - 1]), bd_geom(VE[t - 1]), rc.ray_offset, o);
+                o.c = C;
+                o.pixel = pixel;
+                o.light_prim = -1;
+            } else {
+                film_add(w.film, pixel, C);
+                atomicAdd(&w.ctr->stat_contrib, 1ull);
+            }
+        }
+    }
+    cursor = (n << 8);
+    return true;
+}
+
+// One wavefront step of bdpt. A slot traces its sample's light subpath, then its eye subpath
+// (one extension ray per step), then evaluates its strategies, at most two shadow rays per
+// step. Subpath vertex j is kept in HBM (kBdptMaxVertices per subpath); random numbers of the
+// light subpath use vertex keys 1.., those of the eye subpath 65.., Russian roulette of vertex
+// j on (vbase + j + 1, RNG_NEE_RR).w.
+template <typename R>
+__global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
+        const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
+        uint8_t st = w.state[s];
+        int4 bi = w.bd_info[s];
+        int phase = bi.x & 0xFF;
+        bool pending = ((bi.x >> 8) & 1) != 0;
+        int nL = bi.y, nE = bi.z, cursor = bi.w;
+        BdVert<R>* VL = w.bd_verts + (size_t)s * 2 * kBdptMaxVertices;
+        BdVert<R>* VE = VL + kBdptMaxVertices;
+        unsigned long long sample = w.sample[s];
+        bool need_new = st == SLOT_EMPTY;
+        ShadowRay<R> sh[2];
+        sh[0].valid = sh[1].valid = false;
+
+        if (st == SLOT_ACTIVE) {
+            const RngKey rk = make_rng(rc.seed, sample);
+            if (phase < 2 && pending) {
+                // the extension hit of subpath `phase` (bdpt.hpp:106-129)
+                pending = false;
+                const float4 h = w.hit[s];
+                if (__float_as_int(h.w) >= 0) {
+                    BdVert<R>* V = phase == 0 ? VL : VE;
+                    int& nv = phase == 0 ? nL : nE;
+                    const uint32_t vbase = phase == 0 ? 0u : 64u;
+                    V3<R> d;
+                    Geom<R> g;
+                    const int prim = hit_geometry(sv, rc, w, s, h, d, g, true);
+                    V[nv] = bd_vert(g, prim, sv.mats[prim].type & ~(DT_L | DT_E));
+                    const float rr = rng4(rk, vbase + (uint32_t)nv + 1u, RNG_NEE_RR).w;
+                    nv++;
+                    if (!(rr > 0.5f)) pending = bd_extend(sv, rc, w, s, V, nv, vbase, rk, phase == 0);
+                }
+            }
+            if (phase == 0 && !pending) {
+                phase = 1;
+                bd_first_vertex(sv, VE, 64u, rk, false);
+                nE = 1;
+                pending = bd_extend(sv, rc, w, s, VE, 1, 64u, rk, false);
+            }
+            if (phase == 1 && !pending) {
+                phase = 2;
+                cursor = 2 << 8;
+            }
+            if (phase == 2) {
+                if (bd_connect(sv, rc, w, VL, VE, nL, nE, cursor, sh)) {
+                    need_new = true;
+                    st = SLOT_EMPTY;
+                }
+            }
+        }
+
+        // ---- claim a new sample: its light subpath starts here ----
+        {
+            const unsigned mask = __ballot_sync(0xFFFFFFFFu, need_new);
+            unsigned long long k = 0;
+            if (mask != 0u) {
+                const int leader = __ffs(mask) - 1;
+                unsigned long long b = 0;
+                if ((int)lane_id() == leader) b = atomicAdd(&w.ctr->next_sample, (unsigned long long)__popc(mask));
+                b = __shfl_sync(0xFFFFFFFFu, b, leader);
+                k = b + (unsigned long long)__popc(mask & lanemask_lt());
+            }
+            if (need_new) {
+                if (k >= (unsigned long long)rc.num_samples) {
+                    st = SLOT_DONE;
+                } else {
+                    sample = (unsigned long long)rc.sample_offset + k;
+                    const RngKey rk = make_rng(rc.seed, sample);
+                    bd_first_vertex(sv, VL, 0u, rk, true);
+                    nL = 1;
+                    nE = 0;
+                    phase = 0;
+                    pending = bd_extend(sv, rc, w, s, VL, 1, 0u, rk, true);
+                    if (!pending) {
+                        phase = 1;
+                        bd_first_vertex(sv, VE, 64u, rk, false);
+                        nE = 1;
+                        pending = bd_extend(sv, rc, w, s, VE, 1, 64u, rk, false);
+                        if (!pending) {
+                            phase = 2;  // evaluated from the next step on
+                            cursor = 2 << 8;
+                        }
+                    }
+                    st = SLOT_ACTIVE;
+                }
+            }
+            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+        }
+        w.state[s] = st;
+        w.sample[s] = sample;
+        w.bd_info[s] = make_int4(phase | (pending ? 0x100 : 0), nL, nE, cursor);
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const int q = warp_append(&w.ctr->sh_count, sh[r].valid);
+            if (sh[r].valid) {
+                w.sh_o[q] = make_float4(sh[r].ox, sh[r].oy, sh[r].oz, sh[r].tmin);
+                w.sh_d[q] = make_float4(sh[r].dx, sh[r].dy, sh[r].dz, sh[r].tmax);
+                w.sh_c[q] = Vec4T<R>{sh[r].c.x, sh[r].c.y, sh[r].c.z, R(0)};
+                w.sh_pix[q] = sh[r].pixel;
+            }
+        }
+        {
+            const bool want_ext = st == SLOT_ACTIVE && pending;
+            const int q = warp_append(&w.ctr->ext_count, want_ext);
+            if (want_ext) w.ext_queue[q] = s;
+        }
+        {
+            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
+            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
+        }
+    }
+}
+
+// Which logic kernel a wave runs.
+constexpr int kLogicCamera = 0, kLogicLight = 1, kLogicBdpt = 2;
+
 // Adds a per-thread traversal count into a global counter with one atomic per warp.
 NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
     unsigned long long x = v;
@@ -1326,7 +1574,7 @@ struct TraceGrids {
     }
 };
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, bool LIGHT = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
                        int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev,
                        const JobView<R>* jobs = nullptr, int num_jobs = 0) {
@@ -1338,7 +1586,9 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     cudaMemsetAsync((char*)ctr + off, 0, len, stream);
     if (ev) cudaEventRecord(ev[0], stream);
     const size_t adj_bytes = (ADJ && rc.num_prims <= kAdjSmemPrims) ? 6 * sizeof(float) * rc.num_prims : 0;
-    if constexpr (LIGHT)
+    if constexpr (LOGIC == kLogicBdpt)
+        k_logic_bdpt<R><<<g_logic, 256, 0, stream>>>(sv, v, rc);
+    else if constexpr (LOGIC == kLogicLight)
         k_logic_lt<R, DIRECT><<<g_logic, 256, 0, stream>>>(sv, v, rc);
     else
         k_logic<R, DIRECT, ADJ, BATCH><<<g_logic, 256, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc, jobs, num_jobs);
@@ -1353,7 +1603,7 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     if (ev) cudaEventRecord(ev[3], stream);
 }
 
-template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, bool LIGHT = false>
+template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
               bool kernel_timing, cudaStream_t stream, const JobView<R>* jobs = nullptr, int num_jobs = 0) {
     DeviceScene& ds = *hs.dev;
@@ -1371,7 +1621,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         cudaGraph_t graph = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < iters_per_graph; it++)
-            enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LIGHT>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
+            enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LOGIC>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
                                                                    nullptr, jobs, num_jobs);
         const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
         if (cap != cudaSuccess) {
@@ -1390,14 +1640,17 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     // Each path ends within (max vertices) iterations after it starts; the bound below is
     // generous and only guards against a logic error spinning forever.
     const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
-    const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
+    const long long mv = rc.max_vertices > 0 ? rc.max_vertices : (LOGIC == kLogicBdpt ? kBdptMaxVertices : 4096);
+    // bdpt: two subpaths, then its strategies two at a time
+    const long long per_path = LOGIC == kLogicBdpt ? 2 * mv + mv * mv + 8 : mv + 2;
+    const long long max_iters = per_slot * per_path + 64;
     try {
         if (kernel_timing)
             for (auto& e : kev) CUDA_CHECK(cudaEventCreate(&e));
         CUDA_CHECK(cudaEventRecord(wv->ev0, stream));
         while (true) {
             if (kernel_timing) {
-                enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LIGHT>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
+                enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LOGIC>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
                                                                        kev, jobs, num_jobs);
                 CUDA_CHECK(cudaGetLastError());
                 CUDA_CHECK(cudaEventSynchronize(kev[3]));
@@ -1455,6 +1708,25 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
 
 }  // namespace
 
+namespace {
+
+// Per-slot subpath vertices and cursors of bdpt, allocated with the wave the first time it runs bdpt.
+template <typename R>
+void ensure_bdpt_buffers(RenderWave* wv, WaveView<R>& v) {
+    if (wv->bdpt_precision >= 0) return;
+    void* a = nullptr;
+    void* b = nullptr;
+    CUDA_CHECK(cudaMalloc(&a, sizeof(BdVert<R>) * 2 * kBdptMaxVertices * (size_t)wv->Q));
+    wv->bufs.push_back(a);
+    CUDA_CHECK(cudaMalloc(&b, sizeof(int4) * (size_t)wv->Q));
+    wv->bufs.push_back(b);
+    v.bd_verts = (BdVert<R>*)a;
+    v.bd_info = (int4*)b;
+    wv->bdpt_precision = wv->precision;
+}
+
+}  // namespace
+
 void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cudaStream_t user_stream) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
@@ -1465,7 +1737,9 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     cudaStream_t stream = user_stream ? user_stream : ds.stream;
     ds.last_stats = ngi_render_stats{};
     if (p.num_samples == 0) return;
-    int Q = p.wave_size > 0 ? p.wave_size : (1 << 22);
+    const bool bdpt = p.renderer == NGI_RENDERER_BDPT;
+    // bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): a smaller default wave
+    int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (1 << 22));
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
@@ -1490,17 +1764,29 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT || p.renderer == NGI_RENDERER_LTDIRECT;
     const bool light = p.renderer == NGI_RENDERER_LT || p.renderer == NGI_RENDERER_LTDIRECT;
-    if (light) {
+    if (bdpt) {
+        if (p.precision == NGI_PRECISION_FP64) {
+            ensure_bdpt_buffers<double>(wv, wv->vd);
+            WaveView<double> v = wv->vd;
+            v.film = d_film;
+            run_wave<double, false, false, false, false, kLogicBdpt>(hs, wv, v, rc, ipg, timing, stream);
+        } else {
+            ensure_bdpt_buffers<float>(wv, wv->vf);
+            WaveView<float> v = wv->vf;
+            v.film = d_film;
+            run_wave<float, false, false, false, false, kLogicBdpt>(hs, wv, v, rc, ipg, timing, stream);
+        }
+    } else if (light) {
         if (p.precision == NGI_PRECISION_FP64) {
             WaveView<double> v = wv->vd;
             v.film = d_film;
-            if (direct) run_wave<double, true, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
-            else run_wave<double, false, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            if (direct) run_wave<double, true, false, false, false, kLogicLight>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<double, false, false, false, false, kLogicLight>(hs, wv, v, rc, ipg, timing, stream);
         } else {
             WaveView<float> v = wv->vf;
             v.film = d_film;
-            if (direct) run_wave<float, true, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
-            else run_wave<float, false, false, false, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            if (direct) run_wave<float, true, false, false, false, kLogicLight>(hs, wv, v, rc, ipg, timing, stream);
+            else run_wave<float, false, false, false, false, kLogicLight>(hs, wv, v, rc, ipg, timing, stream);
         }
     } else if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v = wv->vd;

@@ -1042,6 +1042,241 @@ void ProcessSampleLT(RenderCtx& c, Sampler& smp) {
     }
 }
 
+// ---- bdpt: bidirectional path tracing with power-heuristic MIS (include/nanogi/bdpt.hpp) ----------
+
+struct PVert {  // PathVertex (bdpt.hpp:40-45)
+    int type = 0;
+    Geom geom;
+    const Prim* prim = nullptr;
+};
+
+dv3 Dir(const PVert& from, const PVert& to) { return normalize(to.geom.p - from.geom.p); }
+
+// Primitive::EvaluatePosition (rt.hpp:594-641)
+double EvaluatePosition(const Prim& p, bool force) {
+    if (p.d.type & L) return p.d.l_type == 1 ? (force ? 1.0 : 0.0) : 1.0;
+    return p.d.e_type == 1 ? (force ? 1.0 : 0.0) : 1.0;
+}
+
+// Scene::EvaluateEmitterPDF (rt.hpp:2338-2352)
+double EmitterPdf(const ora_scene& s, const Prim& p) {
+    if (p.d.type & L) return 1.0 / (double)s.lights.size();
+    if (p.d.type & E) return 1.0;
+    return 0.0;
+}
+
+// Subpaths keep at most 32 vertices (the reference's are unbounded when max_vertices = -1; with
+// Russian roulette at 1/2 per bounce a longer one has probability 2^-31).
+constexpr int kBdptMaxSubpath = 32;
+
+// Path::SampleSubpath (bdpt.hpp:58-131). Random numbers of step k of a subpath are keyed by
+// vertex vbase + k + 1 (light subpath vbase 0, eye subpath 64): emitter pick and position on
+// CALL_SENSOR, direction on CALL_DIR, Russian roulette on CALL_NEE_RR lane 3.
+void SampleSubpath(RenderCtx& c, Sampler& smp, bool le, uint32_t vbase, std::vector<PVert>& vs) {
+    const ora_scene& s = *c.s;
+    const ora_render_params& P = *c.p;
+    vs.clear();
+    for (int step = 0; (P.max_vertices == -1 || step < P.max_vertices) && step < kBdptMaxSubpath; step++) {
+        const uint32_t key = vbase + (uint32_t)step + 1;
+        if (step == 0) {
+            PVert v;
+            v.type = le ? L : E;
+            const double ue = smp.get(key, CALL_SENSOR, 2);
+            if (le) {
+                const int n = (int)s.lights.size();
+                v.prim = &s.prims[s.lights[std::min(std::max((int)(ue * n), 0), n - 1)]];
+            } else {
+                v.prim = &s.prims[s.sensor];
+            }
+            const double a0 = smp.get(key, CALL_SENSOR, 0), a1 = smp.get(key, CALL_SENSOR, 1);
+            SamplePosition(s, *v.prim, a0, a1, v.geom);
+            vs.push_back(v);
+            continue;
+        }
+        const PVert pv = vs.back();
+        const dv3 wi = vs.size() > 1 ? Dir(pv, vs[vs.size() - 2]) : dv3(0, 0, 0);
+        const double u0 = smp.get(key, CALL_DIR, 0), u1 = smp.get(key, CALL_DIR, 1);
+        const double uc = smp.get(key, CALL_DIR, 2);
+        const dv3 wo = SampleDirection(*pv.prim, u0, u1, uc, pv.type, pv.geom, wi);
+        const dv3 f = EvaluateDirection(*pv.prim, pv.geom, pv.type, wi, wo, le, true);
+        if (is_zero(f)) break;
+        Isect is;
+        c.ext++;
+        float tmin;
+        const dv3 ro = RayOrigin(pv.geom, wo, P.ray_offset, tmin);
+        if (!Intersect(s, P.use_bvh != 0, ro, wo, is, tmin, InfF, P.ray_offset)) break;
+        PVert v;
+        v.geom = is.geom;
+        v.prim = &s.prims[is.prim];
+        v.type = v.prim->d.type & ~Emitter;
+        const double rr = smp.get(key, CALL_NEE_RR, 3);
+        vs.push_back(v);
+        if (rr > 0.5) break;
+    }
+}
+
+// Path::Connect (bdpt.hpp:133-180)
+bool Connect(RenderCtx& c, int s, int t, const std::vector<PVert>& sl, const std::vector<PVert>& se,
+             std::vector<PVert>& x) {
+    x.clear();
+    if (s == 0) {
+        if ((se[t - 1].prim->d.type & L) == 0) return false;
+        for (int i = t - 1; i >= 0; i--) x.push_back(se[i]);
+        x.front().type = L;
+    } else if (t == 0) {
+        if ((sl[s - 1].prim->d.type & E) == 0) return false;
+        for (int i = 0; i < s; i++) x.push_back(sl[i]);
+        x.back().type = E;
+    } else {
+        c.sh++;
+        const Geom& a = sl[s - 1].geom;
+        const Geom& b = se[t - 1].geom;
+        bool vis;
+        if (c.p->ray_offset == 1) vis = VisibleBetween(*c.s, c.p->use_bvh != 0, ToFloat(OffsetPoint(a, b.p - a.p)), OffsetPoint(b, a.p - b.p));
+        else vis = Visible(*c.s, c.p->use_bvh != 0, a.p, b.p);
+        if (!vis) return false;
+        for (int i = 0; i < s; i++) x.push_back(sl[i]);
+        for (int i = t - 1; i >= 0; i--) x.push_back(se[i]);
+    }
+    return true;
+}
+
+// Path::EvaluateCst (bdpt.hpp:213-244)
+dv3 EvaluateCst(const std::vector<PVert>& x, int s) {
+    const int n = (int)x.size(), t = n - s;
+    if (s == 0 && t > 0) {
+        const PVert& v = x[0];
+        return EvaluateDirection(*v.prim, v.geom, v.type, dv3(0, 0, 0), Dir(v, x[1]), false, false) *
+               EvaluatePosition(*v.prim, false);
+    }
+    if (s > 0 && t == 0) {
+        const PVert& v = x[n - 1];
+        return EvaluateDirection(*v.prim, v.geom, v.type, dv3(0, 0, 0), Dir(v, x[n - 2]), true, false) *
+               EvaluatePosition(*v.prim, false);
+    }
+    const PVert& vL = x[s - 1];
+    const PVert& vE = x[s];
+    const dv3 wiL = s - 2 >= 0 ? Dir(vL, x[s - 2]) : dv3(0, 0, 0);
+    const dv3 wiE = s + 1 < n ? Dir(vE, x[s + 1]) : dv3(0, 0, 0);
+    const dv3 fsL = EvaluateDirection(*vL.prim, vL.geom, vL.type, wiL, Dir(vL, vE), true, false);
+    const dv3 fsE = EvaluateDirection(*vE.prim, vE.geom, vE.type, wiE, Dir(vE, vL), false, false);
+    return fsL * GeometryTerm(vL.geom, vE.geom) * fsE;
+}
+
+// f / p with f = 0 -> 0 (LocalContrb, bdpt.hpp:252-257)
+dv3 LocalContrb(dv3 f, double p) { return is_zero(f) ? dv3(0, 0, 0) : f / p; }
+
+// Path::EvaluateUnweightContribution (bdpt.hpp:246-320)
+dv3 EvaluateUnweighted(const ora_scene& sc, const std::vector<PVert>& x, int s) {
+    const int n = (int)x.size(), t = n - s;
+    dv3 aL(1, 1, 1);
+    if (s > 0) {
+        const PVert& v0 = x[0];
+        aL = LocalContrb(dv3(1, 1, 1) * EvaluatePosition(*v0.prim, true), PositionPdf(*v0.prim) * EmitterPdf(sc, *v0.prim));
+        for (int i = 0; i < s - 1; i++) {
+            const PVert& v = x[i];
+            const dv3 wi = i >= 1 ? Dir(v, x[i - 1]) : dv3(0, 0, 0);
+            const dv3 wo = Dir(v, x[i + 1]);
+            aL = aL * LocalContrb(EvaluateDirection(*v.prim, v.geom, v.type, wi, wo, true, true),
+                                  EvaluateDirectionPdf(*v.prim, v.geom, v.type, wi, wo));
+        }
+    }
+    if (is_zero(aL)) return dv3(0, 0, 0);
+    dv3 aE(1, 1, 1);
+    if (t > 0) {
+        const PVert& vn = x[n - 1];
+        aE = LocalContrb(dv3(1, 1, 1) * EvaluatePosition(*vn.prim, true), PositionPdf(*vn.prim) * EmitterPdf(sc, *vn.prim));
+        for (int i = n - 1; i > s; i--) {
+            const PVert& v = x[i];
+            const dv3 wi = i < n - 1 ? Dir(v, x[i + 1]) : dv3(0, 0, 0);
+            const dv3 wo = Dir(v, x[i - 1]);
+            aE = aE * LocalContrb(EvaluateDirection(*v.prim, v.geom, v.type, wi, wo, false, true),
+                                  EvaluateDirectionPdf(*v.prim, v.geom, v.type, wi, wo));
+        }
+    }
+    if (is_zero(aE)) return dv3(0, 0, 0);
+    const dv3 cst = EvaluateCst(x, s);
+    if (is_zero(cst)) return dv3(0, 0, 0);
+    return aL * cst * aE;
+}
+
+// Path::EvaluatePDF (bdpt.hpp:480-529): area-measure pdf of sampling x with strategy s
+double EvaluatePathPdf(const ora_scene& sc, const std::vector<PVert>& x, int s) {
+    if (is_zero(EvaluateCst(x, s))) return 0.0;
+    const int n = (int)x.size(), t = n - s;
+    double pdf = 1.0;
+    if (s > 0) {
+        pdf *= PositionPdf(*x[0].prim) * EmitterPdf(sc, *x[0].prim);
+        for (int i = 0; i < s - 1; i++) {
+            const PVert& v = x[i];
+            const dv3 wi = i - 1 >= 0 ? Dir(v, x[i - 1]) : dv3(0, 0, 0);
+            pdf *= EvaluateDirectionPdf(*v.prim, v.geom, v.type, wi, Dir(v, x[i + 1]));
+            pdf *= GeometryTerm(v.geom, x[i + 1].geom);
+        }
+    }
+    if (t > 0) {
+        pdf *= PositionPdf(*x[n - 1].prim) * EmitterPdf(sc, *x[n - 1].prim);
+        for (int i = n - 1; i >= s + 1; i--) {
+            const PVert& v = x[i];
+            const dv3 wi = i + 1 < n ? Dir(v, x[i + 1]) : dv3(0, 0, 0);
+            pdf *= EvaluateDirectionPdf(*v.prim, v.geom, v.type, wi, Dir(v, x[i - 1]));
+            pdf *= GeometryTerm(v.geom, x[i - 1].geom);
+        }
+    }
+    return pdf;
+}
+
+// Path::EvaluatePowerHeuristicsMISWeightOpt (bdpt.hpp:366-384)
+double MisWeight(const ora_scene& sc, const std::vector<PVert>& x, int s) {
+    const int n = (int)x.size();
+    const double ps = EvaluatePathPdf(sc, x, s);
+    double inv = 0.0;
+    for (int i = 0; i <= n; i++) {
+        const double pi = EvaluatePathPdf(sc, x, i);
+        if (pi > 0) {
+            const double r = pi / ps;
+            inv += r * r;
+        }
+    }
+    return 1.0 / inv;
+}
+
+// Path::SelectionProb (bdpt.hpp:188-202)
+double SelectionProb(int n, int s) {
+    const int t = n - s;
+    double p = 1.0;
+    for (int i = 1; i < s - 1; i++) p *= 0.5;
+    for (int i = t - 2; i >= 1; i--) p *= 0.5;
+    return p;
+}
+
+// ProcessSample_BDPT (src/nanogi.cpp:1133-1194)
+void ProcessSampleBDPT(RenderCtx& c, Sampler& smp, std::vector<PVert>& sl, std::vector<PVert>& se,
+                       std::vector<PVert>& x) {
+    const ora_scene& sc = *c.s;
+    const ora_render_params& P = *c.p;
+    SampleSubpath(c, smp, true, 0, sl);
+    SampleSubpath(c, smp, false, 64, se);
+    c.cam++;
+    const int nL = (int)sl.size(), nE = (int)se.size();
+    for (int n = 2; n <= nE + nL; n++) {
+        if (P.max_vertices != -1 && n > P.max_vertices) continue;
+        for (int s = std::max(0, n - nE); s <= std::min(nL, n); s++) {
+            const int t = n - s;
+            if (!Connect(c, s, t, sl, se, x)) continue;
+            const dv3 Cs = EvaluateUnweighted(sc, x, s);
+            if (is_zero(Cs)) continue;
+            const dv3 C = Cs * MisWeight(sc, x, s) / SelectionProb(n, s);
+            if (is_zero(C)) continue;
+            // Path::RasterPosition (bdpt.hpp:204-211)
+            const PVert& v = x[x.size() - 1];
+            double rx = 0, ry = 0;
+            RasterPosition(*v.prim, Dir(v, x[x.size() - 2]), v.geom, rx, ry);
+            Accumulate(*c.film, PixelIndex(rx, ry, P.width, P.height), C);
+        }
+    }
+}
+
 ora_scene* Build(const ora_prim_desc* prims, int n_prims, const float* tri_pos, const float* tri_nrm,
                  const float* tri_uv, int64_t n_tris, double aspect) {
     auto s = std::make_unique<ora_scene>();
@@ -1161,7 +1396,8 @@ int ora_visible(ora_scene* s, const double* pts, int64_t n, int32_t use_bvh, uin
 int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_render_stats* stats) {
     if (!s || !p || !film_out) { g_err = "NULL argument"; return 1; }
     if (s->sensor < 0) { g_err = "no sensor"; return 1; }
-    if (p->renderer < 0 || p->renderer > 3) { g_err = "unknown renderer"; return 1; }
+    if (p->renderer < 0 || p->renderer > 4) { g_err = "unknown renderer"; return 1; }
+
     if (p->renderer >= 1 && s->lights.empty()) { g_err = "this renderer needs a light"; return 1; }
     const size_t elems = 3 * (size_t)p->width * p->height;
     int threads = p->num_threads > 0 ? p->num_threads : (int)std::thread::hardware_concurrency();
@@ -1183,6 +1419,7 @@ int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_r
         c.p = p;
         c.film = &films[tid];
         c.strat_end = strat_end;
+        std::vector<PVert> sl, se, x;  // bdpt subpaths and full path, reused per sample
         std::mt19937 eng(seeds[tid]);
         std::uniform_real_distribution<double> dist;
         Sampler smp;
@@ -1198,7 +1435,8 @@ int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_r
             for (int64_t k = b; k < e; k++) {
                 smp.sample = (uint64_t)(p->sample_offset + k);
                 smp.cache_vertex = 0xFFFFFFFFu;
-                if (p->renderer >= 2) ProcessSampleLT(c, smp);
+                if (p->renderer == 4) ProcessSampleBDPT(c, smp, sl, se, x);
+                else if (p->renderer >= 2) ProcessSampleLT(c, smp);
                 else ProcessSample(c, smp);
             }
         }

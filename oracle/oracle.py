@@ -237,7 +237,7 @@ class OracleScene:
     def render(self, renderer="pt", num_samples=1000, max_vertices=-1, width=16, height=16, seed=0,
                sample_offset=0, rng_mode="replay", raster="stratified", threads=0, use_bvh=True, grain=1000,
                ray_offset="reference"):
-        p = RenderParams(renderer={"pt": 0, "ptdirect": 1, "lt": 2, "ltdirect": 3}[renderer], max_vertices=max_vertices,
+        p = RenderParams(renderer={"pt": 0, "ptdirect": 1, "lt": 2, "ltdirect": 3, "bdpt": 4}[renderer], max_vertices=max_vertices,
                          num_samples=num_samples, width=width, height=height, seed=seed & 0xFFFFFFFFFFFFFFFF,
                          sample_offset=sample_offset, rng_mode={"reference": 0, "replay": 1}[rng_mode],
                          raster_mode={"stratified": 0, "uniform": 1}[raster], num_threads=threads,

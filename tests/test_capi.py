@@ -147,7 +147,7 @@ def test_cli_usage_and_errors(native_lib, tmp_path):
     cli = ROOT / "nanogi_gb300" / "_build" / "nanogi"
     r = subprocess.run([str(cli)], capture_output=True, text=True)
     assert r.returncode != 0 and "Usage: nanogi" in r.stdout
-    r = subprocess.run([str(cli), "bdpt", "x.yml", "o.hdr", "4", "4"], capture_output=True, text=True)
+    r = subprocess.run([str(cli), "ptmnee", "x.yml", "o.hdr", "4", "4"], capture_output=True, text=True)
     assert r.returncode != 0 and "not built" in r.stderr
     r = subprocess.run([str(cli), "pt", str(tmp_path / "none.yml"), "o.hdr", "4", "4"], capture_output=True, text=True)
     assert r.returncode != 0 and "ERROR" in r.stderr

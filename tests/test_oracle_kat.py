@@ -292,3 +292,18 @@ def test_constant_textures_render_like_constant_albedo(oracle_lib):
         a = OracleScene.from_desc(plain, 1.0).render(r, **kw)
         b = OracleScene.from_desc(tex, 1.0).render(r, **kw)
         assert np.array_equal(a, b), r  # one thread: the same summation order
+
+
+def test_oracle_bdpt_matches_pt_with_area_lights(oracle_lib):
+    """bdpt (bdpt.hpp) and pt estimate the same image when every light is an area light."""
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    o = OracleScene.from_desc(scenegen.material_box(with_point=False, with_directional=False), 1.0)
+    W = H = 8
+    kw = dict(num_samples=W * H * 4096, max_vertices=8, width=W, height=H, rng_mode="reference")
+    pt = o.render("pt", seed=1, **kw)
+    pt2 = o.render("pt", seed=2, **kw)
+    b = o.render("bdpt", seed=3, **kw)
+    assert abs(b.sum() / pt.sum() - 1) < 0.03
+    assert np.sqrt(((b - pt) ** 2).sum()) < 1.5 * np.sqrt(((pt2 - pt) ** 2).sum())
