@@ -181,10 +181,10 @@ def measured_peak():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of k_extend from the committed ncu summary, if any."""
+    """Per-launch DRAM bytes of the extension k_trace from the committed ncu summary, if any."""
     import re
 
-    p = ROOT / "profiles" / "k_extend_terrain_small.md"
+    p = ROOT / "profiles" / "k_trace_terrain_small.md"
     if WORKLOAD == "terrain" and p.exists():
         m = re.search(r"^dram_bytes_per_launch:\s*(\d+)", p.read_text(), re.M)
         if m:
