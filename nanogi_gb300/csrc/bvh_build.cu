@@ -3,13 +3,14 @@
 // Replaces the Embree build of include/nanogi/rt.hpp:2087-2143. Pipeline (all on device):
 //   1. per-triangle bounds and centroid bounds
 //   2. 63-bit Morton codes of the centroids, radix sort (CUB)
-//   3. binary radix tree (Karras, HPG 2012), one thread per internal node
-//   4. bottom-up bounds refit with per-node arrival counters
-//   5. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017):
+//   3. binary tree: PLOC clustering of the sorted leaves (Meister and Bittner 2018), leaves
+//      renumbered depth-first so every subtree is a contiguous range; or, with NGI_BVH_PLOC=0,
+//      the binary radix tree (Karras, HPG 2012) and a bottom-up bounds refit
+//   4. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017):
 //      each node greedily opens its largest-area internal child until it has 8 children,
 //      subtrees of <= 3 triangles become leaves, children are assigned to slots by ray
 //      octant, and child boxes are quantised to 8 bits per plane relative to the parent.
-//   6. triangles, normals and uvs are gathered into leaf order.
+//   5. triangles, normals and uvs are gathered into leaf order.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -27,6 +28,7 @@ namespace {
 
 constexpr int kLeafMax = 3;   // triangles per leaf child (unary count field holds 1..3)
 constexpr uint32_t kLeafFlag = 0x80000000u;
+const int kNoParent = -1;
 
 #define BVH_CHECK(x)                                                                          \
     do {                                                                                      \
@@ -182,6 +184,187 @@ __global__ void k_refit(int n, const uint32_t* __restrict__ sorted_tri, const fl
         __threadfence();
         p = int_parent[p];
     }
+}
+
+// ---- PLOC: parallel locally-ordered clustering (Meister and Bittner, TVCG 2018) --------------
+// Clusters start as the Morton-sorted leaves. Each round every cluster finds, within R positions
+// on either side, the cluster whose merged box has the least surface area; mutual nearest
+// neighbours merge into a new internal node at the lower position, and the array is compacted.
+// The binary tree this yields has a lower SAH cost than the radix tree of the same keys.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__device__ __forceinline__ float merged_area(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    const float x = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
+    const float y = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
+    const float z = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+    return x * y + y * z + z * x;
+}
+
+__global__ void k_leaf_gather(int n, const uint32_t* __restrict__ sorted_tri, const float4* __restrict__ tlo,
+                              const float4* __restrict__ thi, float4* __restrict__ leaf_lo,
+                              float4* __restrict__ leaf_hi, uint32_t* __restrict__ cl_ref) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t t = sorted_tri[j];
+    leaf_lo[j] = tlo[t];
+    leaf_hi[j] = thi[t];
+    cl_ref[j] = kLeafFlag | (uint32_t)j;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(int count, const float4* __restrict__ lo,
+                                                        const float4* __restrict__ hi, int* __restrict__ nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const int base = blockIdx.x * kPlocBlock - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+        const int j = base + k;
+        if (j >= 0 && j < count) {
+            slo[k] = lo[j];
+            shi[k] = hi[j];
+        }
+    }
+    __syncthreads();
+    const int i = blockIdx.x * kPlocBlock + threadIdx.x;
+    if (i >= count) return;
+    const int li = threadIdx.x + kPlocRadius;
+    float best = INFINITY;
+    int bj = -1;
+    for (int d = -kPlocRadius; d <= kPlocRadius; d++) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= count) continue;
+        const float a = merged_area(slo[li], shi[li], slo[li + d], shi[li + d]);
+        if (a < best || bj < 0) {  // strict: the lower index wins ties
+            best = a;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+// merge[i] = 1 where i starts a new internal node (mutual pair, lower index), keep[i] = 1 where
+// position i survives the round (unmerged, or the new node).
+__global__ void k_ploc_flags(int count, const int* __restrict__ nn, int* __restrict__ merge, int* __restrict__ keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > count) return;
+    if (i == count) {  // the scans' total entries
+        merge[i] = 0;
+        keep[i] = 0;
+        return;
+    }
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    merge[i] = mutual && i < j ? 1 : 0;
+    keep[i] = mutual && i > j ? 0 : 1;
+}
+
+__global__ void k_ploc_merge(int count, const int* __restrict__ nn, const int* __restrict__ merge_off,
+                             const int* __restrict__ keep_off, const uint32_t* __restrict__ ref,
+                             const float4* __restrict__ lo, const float4* __restrict__ hi, uint32_t node_base,
+                             uint32_t* __restrict__ left, uint32_t* __restrict__ right, float4* __restrict__ int_lo,
+                             float4* __restrict__ int_hi, int* __restrict__ int_parent, int* __restrict__ leaf_parent,
+                             uint32_t* __restrict__ out_ref, float4* __restrict__ out_lo, float4* __restrict__ out_hi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    if (mutual && i > j) return;  // merged into the pair's lower position
+    const int dst = keep_off[i];
+    if (!mutual) {
+        out_ref[dst] = ref[i];
+        out_lo[dst] = lo[i];
+        out_hi[dst] = hi[i];
+        return;
+    }
+    const uint32_t node = node_base + (uint32_t)merge_off[i];
+    const uint32_t a = ref[i], b = ref[j];
+    const float4 alo = lo[i], ahi = hi[i], blo = lo[j], bhi = hi[j];
+    const float4 mlo = make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.0f);
+    const float4 mhi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.0f);
+    left[node] = a;
+    right[node] = b;
+    int_lo[node] = mlo;
+    int_hi[node] = mhi;
+    if (a & kLeafFlag) leaf_parent[a & ~kLeafFlag] = (int)node; else int_parent[a] = (int)node;
+    if (b & kLeafFlag) leaf_parent[b & ~kLeafFlag] = (int)node; else int_parent[b] = (int)node;
+    out_ref[dst] = node;
+    out_lo[dst] = mlo;
+    out_hi[dst] = mhi;
+}
+
+// Leaf counts of every internal node, bottom-up (the second child to arrive computes its parent).
+__global__ void k_subtree_counts(int n, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                                 const int* __restrict__ int_parent, const int* __restrict__ leaf_parent,
+                                 int* count, int* __restrict__ arrivals, int* __restrict__ error_flag) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int p = leaf_parent[j];
+    for (int steps = 0; p >= 0; steps++) {
+        if (steps > 4096) { atomicOr(error_flag, 1); return; }
+        if (atomicAdd(&arrivals[p], 1) == 0) return;
+        __threadfence();
+        const uint32_t l = left[p], r = right[p];
+        const int cl = (l & kLeafFlag) ? 1 : __ldcg(&count[l]);
+        const int cr = (r & kLeafFlag) ? 1 : __ldcg(&count[r]);
+        __stcg(&count[p], cl + cr);
+        __threadfence();
+        p = int_parent[p];
+    }
+}
+
+// Depth-first position of a subtree: the leaves of the left siblings along its path to the root.
+__device__ __forceinline__ int dfs_offset(uint32_t c, int p, const uint32_t* __restrict__ left,
+                                          const uint32_t* __restrict__ right, const int* __restrict__ int_parent,
+                                          const int* __restrict__ count, int* __restrict__ error_flag) {
+    int pos = 0;
+    for (int steps = 0; p >= 0; steps++) {
+        if (steps > 4096) { atomicOr(error_flag, 1); return 0; }
+        if (right[p] == c) {
+            const uint32_t l = left[p];
+            pos += (l & kLeafFlag) ? 1 : count[l];
+        }
+        c = (uint32_t)p;
+        p = int_parent[p];
+    }
+    return pos;
+}
+
+__global__ void k_dfs_positions(int n, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                                const int* __restrict__ int_parent, const int* __restrict__ leaf_parent,
+                                const int* __restrict__ count, int* __restrict__ leaf_pos, uint8_t* __restrict__ leaf_side,
+                                int2* __restrict__ range, int* __restrict__ error_flag) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        const int p = leaf_parent[j];
+        leaf_pos[j] = dfs_offset(kLeafFlag | (uint32_t)j, p, left, right, int_parent, count, error_flag);
+        leaf_side[j] = (p >= 0 && right[p] == (kLeafFlag | (uint32_t)j)) ? 1 : 0;
+    }
+    if (j < n) {
+        if (leaf_pos[j] < 0 || leaf_pos[j] >= n) atomicOr(error_flag, 1);
+    }
+    if (j < n - 1) {
+        const int first = dfs_offset((uint32_t)j, int_parent[j], left, right, int_parent, count, error_flag);
+        range[j] = make_int2(first, first + count[j] - 1);
+        if (first < 0 || first + count[j] > n) atomicOr(error_flag, 1);
+    }
+}
+
+// Leaves renumbered by depth-first position, so every subtree is one contiguous range.
+__global__ void k_dfs_remap(int n, const int* __restrict__ leaf_pos, const uint8_t* __restrict__ leaf_side,
+                            const int* __restrict__ leaf_parent,
+                            const uint32_t* __restrict__ sorted_tri, const float4* __restrict__ leaf_lo,
+                            const float4* __restrict__ leaf_hi, uint32_t* __restrict__ left, uint32_t* __restrict__ right,
+                            uint32_t* __restrict__ tri_out, float4* __restrict__ lo_out, float4* __restrict__ hi_out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int q = leaf_pos[j];
+    if (q < 0 || q >= n) return;  // only a malformed tree (reported by k_dfs_positions) gets here
+    tri_out[q] = sorted_tri[j];
+    lo_out[q] = leaf_lo[j];
+    hi_out[q] = leaf_hi[j];
+    const int p = leaf_parent[j];
+    if (p < 0) return;
+    if (leaf_side[j]) right[p] = kLeafFlag | (uint32_t)q;
+    else left[p] = kLeafFlag | (uint32_t)q;
 }
 
 struct BinView {
@@ -407,6 +590,90 @@ T* dev_alloc(size_t count, std::vector<void*>& temps) {
 
 }  // namespace
 
+// PLOC against the radix tree of the same Morton keys: terrain 1322 vs 1305 Mrays/s (12.5 nodes
+// and 4.7 triangles per ray against 12.1 and 4.8); the 10M-triangle interior halves its work per
+// ray (30 nodes and 15 triangles against 55 and 30). Build: 8 ms for 1.55M triangles, 20 ms for 10M.
+#ifndef NGI_BVH_PLOC
+#define NGI_BVH_PLOC 1
+#endif
+constexpr bool kUsePloc = NGI_BVH_PLOC != 0;
+
+// PLOC binary tree over the Morton-sorted leaves, then depth-first leaf positions so that every
+// subtree is a contiguous range (what the 8-wide collapse reads). Fills the same arrays as the
+// radix tree + refit path and returns the root's reference. leaf_tri receives the triangle of
+// each depth-first leaf position.
+uint32_t BuildPloc(int n, const uint32_t* sorted_tri, const float4* tlo, const float4* thi, uint32_t* left,
+                   uint32_t* right, int* int_parent, int* leaf_parent, int2* range, float4* leaf_lo, float4* leaf_hi,
+                   float4* int_lo, float4* int_hi, int* arrivals, uint32_t*& leaf_tri, std::vector<void*>& temps,
+                   cudaStream_t stream) {
+    const int T = 256;
+    const int nb = (n + T - 1) / T;
+    float4* mlo = dev_alloc<float4>(n, temps);  // leaf boxes in Morton order
+    float4* mhi = dev_alloc<float4>(n, temps);
+    uint32_t* ref_a = dev_alloc<uint32_t>(n, temps);
+    uint32_t* ref_b = dev_alloc<uint32_t>(n, temps);
+    float4* lo_a = dev_alloc<float4>(n, temps);
+    float4* hi_a = dev_alloc<float4>(n, temps);
+    float4* lo_b = dev_alloc<float4>(n, temps);
+    float4* hi_b = dev_alloc<float4>(n, temps);
+    int* nn = dev_alloc<int>(n, temps);
+    int* merge = dev_alloc<int>(n + 1, temps);
+    int* keep = dev_alloc<int>(n + 1, temps);
+    int* merge_off = dev_alloc<int>(n + 1, temps);
+    int* keep_off = dev_alloc<int>(n + 1, temps);
+    size_t scan_bytes = 0;
+    BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, merge, merge_off, n + 1, stream));
+    void* scan_tmp = dev_alloc<uint8_t>(scan_bytes, temps);
+    k_leaf_gather<<<nb, T, 0, stream>>>(n, sorted_tri, tlo, thi, mlo, mhi, ref_a);
+    BVH_CHECK(cudaMemcpyAsync(lo_a, mlo, sizeof(float4) * n, cudaMemcpyDeviceToDevice, stream));
+    BVH_CHECK(cudaMemcpyAsync(hi_a, mhi, sizeof(float4) * n, cudaMemcpyDeviceToDevice, stream));
+    int count = n;
+    uint32_t node_base = 0;
+    for (int round = 0; count > 1; round++) {
+        if (round > n) throw DeviceError("PLOC clustering made no progress");
+        const int gb = (count + T - 1) / T;
+        k_ploc_nn<<<(count + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, stream>>>(count, lo_a, hi_a, nn);
+        k_ploc_flags<<<(count + 1 + T - 1) / T, T, 0, stream>>>(count, nn, merge, keep);
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, merge, merge_off, count + 1, stream));
+        BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, keep, keep_off, count + 1, stream));
+        k_ploc_merge<<<gb, T, 0, stream>>>(count, nn, merge_off, keep_off, ref_a, lo_a, hi_a, node_base, left, right,
+                                          int_lo, int_hi, int_parent, leaf_parent, ref_b, lo_b, hi_b);
+        BVH_CHECK(cudaGetLastError());
+        int totals[2];
+        BVH_CHECK(cudaMemcpyAsync(&totals[0], merge_off + count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        BVH_CHECK(cudaMemcpyAsync(&totals[1], keep_off + count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        BVH_CHECK(cudaStreamSynchronize(stream));
+        if (totals[0] <= 0 || totals[1] >= count) throw DeviceError("PLOC clustering made no progress");
+        node_base += (uint32_t)totals[0];
+        count = totals[1];
+        std::swap(ref_a, ref_b);
+        std::swap(lo_a, lo_b);
+        std::swap(hi_a, hi_b);
+    }
+    if (node_base != (uint32_t)(n - 1)) throw DeviceError("PLOC produced a malformed tree");
+    const uint32_t root = node_base - 1;  // the last merge
+    BVH_CHECK(cudaMemcpyAsync(int_parent + root, &kNoParent, sizeof(int), cudaMemcpyHostToDevice, stream));
+    // subtree sizes, depth-first positions, contiguous ranges
+    const int ni = n - 1;
+    int* count_arr = dev_alloc<int>(ni, temps);
+    int* leaf_pos = dev_alloc<int>(n, temps);
+    uint8_t* leaf_side = dev_alloc<uint8_t>(n, temps);
+    BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));
+    k_subtree_counts<<<nb, T, 0, stream>>>(n, left, right, int_parent, leaf_parent, count_arr, arrivals, arrivals + ni);
+    k_dfs_positions<<<nb, T, 0, stream>>>(n, left, right, int_parent, leaf_parent, count_arr, leaf_pos, leaf_side, range,
+                                          arrivals + ni);
+    uint32_t* dfs_tri = dev_alloc<uint32_t>(n, temps);
+    k_dfs_remap<<<nb, T, 0, stream>>>(n, leaf_pos, leaf_side, leaf_parent, sorted_tri, mlo, mhi, left, right, dfs_tri,
+                                      leaf_lo, leaf_hi);
+    BVH_CHECK(cudaGetLastError());
+    int err = 0;
+    BVH_CHECK(cudaMemcpyAsync(&err, arrivals + ni, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    BVH_CHECK(cudaStreamSynchronize(stream));
+    if (err) throw DeviceError("PLOC tree deeper than the walk limit");
+    leaf_tri = dfs_tri;
+    return root;
+}
+
 // Builds the BVH of the n triangles in d_pos (9 floats each, original order).
 void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const float* d_uv, const int* d_tri_prim,
               int n, cudaStream_t stream) {
@@ -453,18 +720,26 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             float4* int_hi = dev_alloc<float4>(ni, temps);
             int* arrivals = dev_alloc<int>(ni + 1, temps);  // last entry: error flag
             BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));
+            uint32_t root_ref = n == 1 ? (kLeafFlag | 0u) : 0u;
+            uint32_t* leaf_tri = vals_s;  // triangle of each leaf position
             if (n == 1) {
                 BVH_CHECK(cudaMemsetAsync(leaf_parent, 0xFF, sizeof(int), stream));  // -1
-            } else {
-                k_radix_tree<<<(n - 1 + T - 1) / T, T, 0, stream>>>(keys_s, n, left, right, int_parent, leaf_parent, range);
             }
-            k_refit<<<nb, T, 0, stream>>>(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, leaf_lo, leaf_hi,
-                                         int_lo, int_hi, arrivals, arrivals + ni);
-            BVH_CHECK(cudaGetLastError());
-            int refit_err = 0;
-            BVH_CHECK(cudaMemcpyAsync(&refit_err, arrivals + ni, sizeof(int), cudaMemcpyDeviceToHost, stream));
-            BVH_CHECK(cudaStreamSynchronize(stream));
-            if (refit_err) throw DeviceError("BVH refit walked past the maximum tree depth");
+            if (n > 1 && kUsePloc) {
+                root_ref = BuildPloc(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, range, leaf_lo, leaf_hi,
+                                     int_lo, int_hi, arrivals, leaf_tri, temps, stream);
+            } else {
+                if (n > 1)
+                    k_radix_tree<<<(n - 1 + T - 1) / T, T, 0, stream>>>(keys_s, n, left, right, int_parent, leaf_parent,
+                                                                     range);
+                k_refit<<<nb, T, 0, stream>>>(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, leaf_lo,
+                                             leaf_hi, int_lo, int_hi, arrivals, arrivals + ni);
+                BVH_CHECK(cudaGetLastError());
+                int refit_err = 0;
+                BVH_CHECK(cudaMemcpyAsync(&refit_err, arrivals + ni, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                BVH_CHECK(cudaStreamSynchronize(stream));
+                if (refit_err) throw DeviceError("BVH refit walked past the maximum tree depth");
+            }
 
             // 8-wide collapse, one level per iteration.
             const size_t max_nodes = (size_t)ni + 1;
@@ -485,7 +760,7 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, n_int, int_off, (int)max_nodes + 1, stream));
             void* scan_tmp = dev_alloc<uint8_t>(scan_bytes, temps);
 
-            const WorkItem root{n == 1 ? (kLeafFlag | 0u) : 0u, 0u};
+            const WorkItem root{root_ref, 0u};
             BVH_CHECK(cudaMemcpyAsync(work_a, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
             BinView bv{left, right, range, leaf_lo, leaf_hi, int_lo, int_hi};
             uint32_t node_count = 1, tri_count = 0;
@@ -499,7 +774,7 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_int, int_off, nwork + 1, stream));
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_tri, tri_off, nwork + 1, stream));
                 k_collapse_emit<<<gb, 128, 0, stream>>>(bv, work_a, nwork, children, int_off, tri_off, node_count,
-                                                       tri_count, vals_s, d_pos, nodes, tris_out, perm, work_b);
+                                                       tri_count, leaf_tri, d_pos, nodes, tris_out, perm, work_b);
                 BVH_CHECK(cudaGetLastError());
                 int totals[2];
                 BVH_CHECK(cudaMemcpyAsync(&totals[0], int_off + nwork, sizeof(int), cudaMemcpyDeviceToHost, stream));

@@ -39,6 +39,12 @@ namespace ngi {
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 
 // Minimum resident blocks per SM asked of the traversal kernels (register budget).
+// Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
+// FP32 logic at 128 registers (25% occupancy); 4 caps it at 64 registers with ~250 B of spills
+// to L1, and was faster on the terrain (1384 vs 1322 Mrays/s): the kernel waits on HBM.
+#ifndef NGI_LOGIC_MIN_BLOCKS
+#define NGI_LOGIC_MIN_BLOCKS 4
+#endif
 #ifndef NGI_TRACE_MIN_BLOCKS
 #define NGI_TRACE_MIN_BLOCKS 8
 #endif
@@ -421,7 +427,7 @@ NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const Wav
 }
 
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false>
-__global__ void __launch_bounds__(256) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
+__global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
                                                const JobView<R>* __restrict__ jobs, int num_jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && !DIRECT && rc0.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
@@ -1738,8 +1744,9 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     ds.last_stats = ngi_render_stats{};
     if (p.num_samples == 0) return;
     const bool bdpt = p.renderer == NGI_RENDERER_BDPT;
-    // bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): a smaller default wave
-    int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (1 << 22));
+    // 2^23 path slots (~0.9 GB FP32): on the terrain 1356 Mrays/s against 1322 at 2^22 and 1318
+    // at 2^24. bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): 2^18.
+    int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (1 << 23));
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
@@ -2171,7 +2178,7 @@ void render_batch(std::vector<HostScene*>& scenes, const std::vector<ngi_render_
             };
             measure(cfg);  // warm: kernels, graphs, wave allocation
             double best = measure(cfg);
-            const int waves[] = {1 << 20, 1 << 21, 1 << 22};
+            const int waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
             for (int wv : waves) {
                 if (wv == cfg.wave || wv > std::max<long long>(trial_total, 256) * 2) continue;
                 BatchConfig c = cfg;
