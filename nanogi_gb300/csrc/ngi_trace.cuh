@@ -94,6 +94,10 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 #ifndef NGI_WHILE_WHILE
 #define NGI_WHILE_WHILE 1
 #endif
+#ifndef NGI_SPECULATIVE
+#define NGI_SPECULATIVE 1
+#endif
+constexpr bool kSpeculative = NGI_SPECULATIVE != 0;
 
 struct TraceStats {
     uint32_t nodes;
@@ -257,10 +261,13 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
         // node phase: every lane without triangles visits nodes until all lanes hold triangles or
         // have run out of nodes
         const unsigned act = __activemask();
-        uint2 tg = make_uint2(0u, 0u);
+        uint2 tg = make_uint2(0u, 0u), tg2 = make_uint2(0u, 0u);
         while (true) {
-            const bool want = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
-            if (!__any_sync(act, want)) break;
+            // speculative (closest hit): a lane holding one triangle group keeps visiting nodes,
+            // into a second group, while some lane of the warp has found none yet
+            const bool needy = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
+            const bool want = (kSpeculative && !ANY_HIT) ? (tg2.y == 0u && s.ngroup.y > 0x00FFFFFFu) : needy;
+            if (!__any_sync(act, needy)) break;
             if (want) {
                 const uint32_t hits = s.ngroup.y;
                 const int bit = 31 - __clz(hits);
@@ -282,11 +289,21 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                 const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
                 if (STATS) stats->nodes++;
                 s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-                tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
-                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
+                const uint2 found = make_uint2(tri_base, hm & 0x00FFFFFFu);
+                if (tg.y == 0u) tg = found;
+                else tg2 = found;
+                if (s.ngroup.y <= 0x00FFFFFFu && found.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
             }
         }
-        while (tg.y != 0u) {
+        if (tg.y == 0u) {
+            tg = tg2;
+            tg2.y = 0u;
+        }
+        while (tg.y != 0u || tg2.y != 0u) {
+            if (tg.y == 0u) {
+                tg = tg2;
+                tg2.y = 0u;
+            }
             const int tb = 31 - __clz(tg.y);
             tg.y &= ~(1u << tb);
             const uint32_t ti = tg.x + (uint32_t)tb;
