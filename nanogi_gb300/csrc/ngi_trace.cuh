@@ -94,8 +94,11 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 #ifndef NGI_WHILE_WHILE
 #define NGI_WHILE_WHILE 1
 #endif
+// Speculative traversal (Aila and Laine 2009): a lane holding triangles keeps visiting nodes
+// into a second group while other lanes search. Measured 1389 vs 1418 Mrays/s on the terrain:
+// off by default.
 #ifndef NGI_SPECULATIVE
-#define NGI_SPECULATIVE 1
+#define NGI_SPECULATIVE 0
 #endif
 constexpr bool kSpeculative = NGI_SPECULATIVE != 0;
 
