@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 
 
-@pytest.mark.parametrize("renderer,ext", [("pt", ".hdr"), ("ptdirect", ".exr"), ("ltdirect", ".png")])
+@pytest.mark.parametrize("renderer,ext", [("pt", ".hdr"), ("ptdirect", ".exr"), ("ltdirect", ".png"), ("bdpt", ".pfm")])
 def test_cli_renders_every_format(native_lib, cornell, tmp_path, renderer, ext):
     _, path = cornell
     out = tmp_path / "out" / f"img{ext}"
