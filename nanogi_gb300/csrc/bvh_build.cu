@@ -447,8 +447,7 @@ __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, in
                                 const uint32_t* __restrict__ children, const int* __restrict__ int_off,
                                 const int* __restrict__ tri_off, uint32_t node_base, uint32_t tri_base_all,
                                 const uint32_t* __restrict__ sorted_tri, const float* __restrict__ pos,
-                                const int* __restrict__ tri_prim, CwNode* __restrict__ nodes,
-                                float4* __restrict__ tris_out,
+                                CwNode* __restrict__ nodes, float4* __restrict__ tris_out,
                                 uint32_t* __restrict__ perm, WorkItem* __restrict__ next_work) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nwork) return;
@@ -553,7 +552,7 @@ __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, in
                 const uint32_t dst = tri_base + (uint32_t)tri_rank + (uint32_t)q;
                 const float* p = pos + 9 * (size_t)tri;
                 tris_out[3 * (size_t)dst + 0] = make_float4(p[0], p[1], p[2], __uint_as_float(tri));
-                tris_out[3 * (size_t)dst + 1] = make_float4(p[3], p[4], p[5], __int_as_float(tri_prim[tri]));
+                tris_out[3 * (size_t)dst + 1] = make_float4(p[3], p[4], p[5], 0.0f);
                 tris_out[3 * (size_t)dst + 2] = make_float4(p[6], p[7], p[8], 0.0f);
                 perm[dst] = tri;
             }
@@ -775,8 +774,7 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_int, int_off, nwork + 1, stream));
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_tri, tri_off, nwork + 1, stream));
                 k_collapse_emit<<<gb, 128, 0, stream>>>(bv, work_a, nwork, children, int_off, tri_off, node_count,
-                                                       tri_count, leaf_tri, d_pos, d_tri_prim, nodes, tris_out, perm,
-                                                       work_b);
+                                                       tri_count, leaf_tri, d_pos, nodes, tris_out, perm, work_b);
                 BVH_CHECK(cudaGetLastError());
                 int totals[2];
                 BVH_CHECK(cudaMemcpyAsync(&totals[0], int_off + nwork, sizeof(int), cudaMemcpyDeviceToHost, stream));

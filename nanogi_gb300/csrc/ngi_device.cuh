@@ -92,7 +92,7 @@ struct DevSensor {
 template <typename R>
 struct SceneView {
     const CwNode* nodes;
-    const float4* tris;        // 3 per triangle, BVH order; p1.w = original triangle id, p2.w = primitive id
+    const float4* tris;        // 3 per triangle, BVH order
     const float4* nrm;         // 3 per triangle, BVH order
     const float2* uv;          // 3 per triangle, BVH order
     const DevMaterial<R>* mats;

@@ -90,17 +90,12 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 // Node phase "while-while" (Aila and Laine 2009): a lane holding triangles waits while the
 // other lanes of its warp keep visiting nodes, so the triangle tests of a warp run together.
 // Measured on the 1.55M-triangle terrain: 1333 Mrays/s against 1105 with one node per step;
-// the single-product box compare adds 0.7%.
+// the single-product box compare adds 0.7%. Measured and not kept: a speculative second
+// triangle group (lanes with triangles visiting nodes while others search; 1389 vs 1418) and a
+// folded quantised-plane form (one subtraction less per plane, boxes two quanta wider; 1010 vs 1076).
 #ifndef NGI_WHILE_WHILE
 #define NGI_WHILE_WHILE 1
 #endif
-// Speculative traversal (Aila and Laine 2009): a lane holding triangles keeps visiting nodes
-// into a second group while other lanes search. Measured 1389 vs 1418 Mrays/s on the terrain:
-// off by default.
-#ifndef NGI_SPECULATIVE
-#define NGI_SPECULATIVE 0
-#endif
-constexpr bool kSpeculative = NGI_SPECULATIVE != 0;
 
 struct TraceStats {
     uint32_t nodes;
@@ -112,16 +107,6 @@ struct TraceStats {
 NGI_D float byte_to_float(uint32_t word, int b) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)) - 8388608.0f;
 }
-
-// 2^23 + byte b of a 32-bit word, as a float (exact): the folded-offset form of byte_to_float.
-NGI_D float byte_bits(uint32_t word, int b) { return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)); }
-
-// The folded form saves one subtraction per plane but widens every box by two quanta; on the
-// 1.55M-triangle terrain it ran 6% slower (1010 vs 1076 Mrays/s), so the exact form is the
-// default.
-#ifndef NGI_FOLDED_BOX
-#define NGI_FOLDED_BOX 0
-#endif
 
 // Packed box test: the near and far plane of an axis are decoded and scaled as one float2
 // through the two-wide FADD2 / FFMA2 instructions of sm_100+. Measured on the 1.55M-triangle
@@ -193,14 +178,6 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
     const float ay = (n0.y - s.rp.oy) * s.idy;
     const float az = (n0.z - s.rp.oz) * s.idz;
     const bool nx = s.dneg & 1u, ny = s.dneg & 2u, nz = s.dneg & 4u;
-#if NGI_FOLDED_BOX
-    // Plane distance of quantised coordinate q: q*s + a. The byte permute yields F = 2^23 + q,
-    // so t = F*s + (a - 2^23 s). The folded addend costs up to one quantum |s| of rounding;
-    // moving near planes 2|s| closer and far planes 2|s| farther keeps every box conservative.
-    const float cx = fmaf(-8388608.0f, sx, ax), cy = fmaf(-8388608.0f, sy, ay), cz = fmaf(-8388608.0f, sz, az);
-    const float mx = 2.0f * fabsf(sx), my = 2.0f * fabsf(sy), mz = 2.0f * fabsf(sz);
-    const float anx = cx - mx, afx = cx + mx, any_ = cy - my, afy = cy + my, anz = cz - mz, afz = cz + mz;
-#endif
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
@@ -218,15 +195,11 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
-#if NGI_PACKED_BOX && !NGI_FOLDED_BOX
+#if NGI_PACKED_BOX
             const float2 px = plane_pair(nearx, farx, j, make_float2(sx, sx), make_float2(ax, ax));
             const float2 py = plane_pair(neary, fary, j, make_float2(sy, sy), make_float2(ay, ay));
             const float2 pz = plane_pair(nearz, farz, j, make_float2(sz, sz), make_float2(az, az));
             const float x0 = px.x, x1 = px.y, y0 = py.x, y1 = py.y, z0 = pz.x, z1 = pz.y;
-#elif NGI_FOLDED_BOX
-            const float x0 = fmaf(byte_bits(nearx, j), sx, anx), x1 = fmaf(byte_bits(farx, j), sx, afx);
-            const float y0 = fmaf(byte_bits(neary, j), sy, any_), y1 = fmaf(byte_bits(fary, j), sy, afy);
-            const float z0 = fmaf(byte_bits(nearz, j), sz, anz), z1 = fmaf(byte_bits(farz, j), sz, afz);
 #else
             const float x0 = fmaf(byte_to_float(nearx, j), sx, ax), x1 = fmaf(byte_to_float(farx, j), sx, ax);
             const float y0 = fmaf(byte_to_float(neary, j), sy, ay), y1 = fmaf(byte_to_float(fary, j), sy, ay);
@@ -264,13 +237,10 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
         // node phase: every lane without triangles visits nodes until all lanes hold triangles or
         // have run out of nodes
         const unsigned act = __activemask();
-        uint2 tg = make_uint2(0u, 0u), tg2 = make_uint2(0u, 0u);
+        uint2 tg = make_uint2(0u, 0u);
         while (true) {
-            // speculative (closest hit): a lane holding one triangle group keeps visiting nodes,
-            // into a second group, while some lane of the warp has found none yet
-            const bool needy = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
-            const bool want = (kSpeculative && !ANY_HIT) ? (tg2.y == 0u && s.ngroup.y > 0x00FFFFFFu) : needy;
-            if (!__any_sync(act, needy)) break;
+            const bool want = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
+            if (!__any_sync(act, want)) break;
             if (want) {
                 const uint32_t hits = s.ngroup.y;
                 const int bit = 31 - __clz(hits);
@@ -292,21 +262,11 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                 const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
                 if (STATS) stats->nodes++;
                 s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-                const uint2 found = make_uint2(tri_base, hm & 0x00FFFFFFu);
-                if (tg.y == 0u) tg = found;
-                else tg2 = found;
-                if (s.ngroup.y <= 0x00FFFFFFu && found.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
+                tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
+                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
             }
         }
-        if (tg.y == 0u) {
-            tg = tg2;
-            tg2.y = 0u;
-        }
-        while (tg.y != 0u || tg2.y != 0u) {
-            if (tg.y == 0u) {
-                tg = tg2;
-                tg2.y = 0u;
-            }
+        while (tg.y != 0u) {
             const int tb = 31 - __clz(tg.y);
             tg.y &= ~(1u << tb);
             const uint32_t ti = tg.x + (uint32_t)tb;

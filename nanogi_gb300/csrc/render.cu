@@ -97,7 +97,6 @@ struct WaveView {
     float4* ray_o;           // extension ray origin (xyz), tmin (w)
     float4* ray_d;           // direction (xyz), tmax (w)
     float4* hit;             // t, u, v, leaf-order triangle index (-1 = miss)
-    int* hit_prim;           // primitive of the hit, so the material load need not wait for the triangle
     Vec4T<R>* thr;           // throughput
     Vec4T<double>* od_o;     // FP64 path: exact origin
     Vec4T<double>* od_d;     // FP64 path: exact direction
@@ -424,7 +423,7 @@ NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const Wav
         g.uvx = R(0);
         g.uvy = R(0);
     }
-    return w.hit_prim[s];
+    return __float_as_int(m1.w);
 }
 
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false>
@@ -1239,7 +1238,6 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                     }
                 } else {
                     w.hit[slot] = make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit));
-                    w.hit_prim[slot] = s.hit >= 0 ? __float_as_int(__ldg(&tris[3 * (size_t)s.hit + 1].w)) : -1;
                 }
                 item = -1;
             }
@@ -1504,7 +1502,6 @@ void alloc_wave_view(RenderWave* wv, WaveView<R>& v, int Q) {
     v.ray_o = (float4*)A(sizeof(float4) * Q);
     v.ray_d = (float4*)A(sizeof(float4) * Q);
     v.hit = (float4*)A(sizeof(float4) * Q);
-    v.hit_prim = (int*)A(sizeof(int) * Q);
     v.thr = (Vec4T<R>*)A(sizeof(Vec4T<R>) * Q);
     if (sizeof(R) == 8) {
         v.od_o = (Vec4T<double>*)A(sizeof(Vec4T<double>) * Q);
@@ -2298,7 +2295,6 @@ size_t carve_wave(unsigned char* base, int Q, WaveView<R>& v) {
     v.ray_o = (float4*)take(sizeof(float4) * Q);
     v.ray_d = (float4*)take(sizeof(float4) * Q);
     v.hit = (float4*)take(sizeof(float4) * Q);
-    v.hit_prim = (int*)take(sizeof(int) * Q);
     v.thr = (Vec4T<R>*)take(sizeof(Vec4T<R>) * Q);
     if (sizeof(R) == 8) {
         v.od_o = (Vec4T<double>*)take(sizeof(Vec4T<double>) * Q);
