@@ -81,6 +81,7 @@ def parse():
     ap.add_argument("--wave-size", type=int, default=0, help="path slots (0 = library default)")
     ap.add_argument("--trace-refill", type=int, default=0, help="traversal refill threshold (0 = default)")
     ap.add_argument("--trace-postpone", type=int, default=0, help="triangle postponing, percent + 1 (0 = default)")
+    ap.add_argument("--iterations-per-graph", type=int, default=0, help="wave iterations per CUDA graph (0 = default)")
     args = ap.parse_args()
     configure(args)
     return args
@@ -287,7 +288,7 @@ def main():
         r = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
                         height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags,
                         wave_size=args.wave_size, trace_refill=args.trace_refill,
-                        trace_postpone=args.trace_postpone)
+                        trace_postpone=args.trace_postpone, iterations_per_graph=args.iterations_per_graph)
         r.render_device(scene, film.data_ptr(), stream.cuda_stream)
         return r.last_stats
 
@@ -354,7 +355,8 @@ def main():
     host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
     r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
                         height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size,
-                        trace_refill=args.trace_refill, trace_postpone=args.trace_postpone)
+                        trace_refill=args.trace_refill, trace_postpone=args.trace_postpone,
+                        iterations_per_graph=args.iterations_per_graph)
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0
