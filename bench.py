@@ -182,14 +182,15 @@ def measured_peak():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the extension k_trace from the committed ncu summary, if any."""
+    """DRAM bytes as a fraction of the traversal kernel's algorithmic bytes, from the committed
+    ncu summary of the terrain workload (applied to the full-size launch), if any."""
     import re
 
     p = ROOT / "profiles" / "k_trace_terrain_small.md"
     if WORKLOAD == "terrain" and p.exists():
-        m = re.search(r"^dram_bytes_per_launch:\s*(\d+)", p.read_text(), re.M)
+        m = re.search(r"^dram_fraction_of_algorithmic:\s*([0-9.]+)", p.read_text(), re.M)
         if m:
-            return {"dram_bytes_per_launch": int(m.group(1))}
+            return float(m.group(1))
     return None
 
 
@@ -330,25 +331,32 @@ def main():
     # ---- per-kernel timing and traversal counters (separate, untimed renders) ----
     st_t = render_step(base, flags=capi.KERNEL_TIMING)
     st_c = render_step(base, flags=capi.TRAVERSAL_COUNTERS)
-    kern = {"k_logic": st_t["logic_ms"], "k_trace<extension>": st_t["extend_ms"],
-            "k_trace<shadow>": st_t["shadow_ms"]}
-    top = max(["k_trace<extension>", "k_trace<shadow>"], key=lambda k: kern[k])
+    ext_bytes = st_c["extension_rays"] * (32 + 16) + 80 * st_c["extend_nodes"] + 48 * st_c["extend_tris"]
+    sh_bytes = st_c["shadow_rays"] * (32 + 4) + 80 * st_c["shadow_nodes"] + 48 * st_c["shadow_tris"]
     launches = st_t["extend_launches"]
-    if top == "k_trace<extension>":
-        rays_k, nodes, tris, out_b = st_c["extension_rays"], st_c["extend_nodes"], st_c["extend_tris"], 16
+    if st_t["shadow_ms"] < 0.01 * st_t["extend_ms"] and st_c["shadow_rays"] > 0:
+        # one traversal launch per iteration traces both queues (no separate shadow launch to time)
+        kern = {"k_logic": st_t["logic_ms"], "k_trace<extension+shadow>": st_t["extend_ms"]}
+        top, alg_bytes = "k_trace<extension+shadow>", ext_bytes + sh_bytes
+        rays_k = st_c["extension_rays"] + st_c["shadow_rays"]
     else:
-        rays_k, nodes, tris, out_b = st_c["shadow_rays"], st_c["shadow_nodes"], st_c["shadow_tris"], 4
-    alg_bytes = rays_k * (32 + out_b) + 80 * nodes + 48 * tris
+        kern = {"k_logic": st_t["logic_ms"], "k_trace<extension>": st_t["extend_ms"],
+                "k_trace<shadow>": st_t["shadow_ms"]}
+        top = max(["k_trace<extension>", "k_trace<shadow>"], key=lambda k: kern[k])
+        alg_bytes = ext_bytes if top == "k_trace<extension>" else sh_bytes
+        rays_k = st_c["extension_rays"] if top == "k_trace<extension>" else st_c["shadow_rays"]
     per_launch_bytes = alg_bytes / max(launches, 1)
     per_launch_ms = kern[top] / max(launches, 1)
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = ncu_traffic()
+    frac_dram = ncu_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None, "kernel": top,
+                "traffic": frac_dram * per_launch_bytes if frac_dram else None, "kernel": top,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
-                "avg_launch_ms": per_launch_ms, "nodes_per_ray": nodes / max(rays_k, 1),
-                "tris_per_ray": tris / max(rays_k, 1),
+                "avg_launch_ms": per_launch_ms,
+                "nodes_per_ray": st_c["extend_nodes"] / max(st_c["extension_rays"], 1),
+                "tris_per_ray": st_c["extend_tris"] / max(st_c["extension_rays"], 1),
+                "traced_rays_per_launch": rays_k / max(launches, 1),
                 "kernel_ms_share": {k: v / max(sum(kern.values()), 1e-9) for k, v in kern.items()}}
 
     # ---- end to end through the host-buffer C ABI entry point ----

@@ -229,9 +229,10 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 // triangles to test, so that tests run together instead of one lane at a time. Returns true
 // when the ray is finished (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is
 // set, and the ray abandoned, if the tree is deeper than the stack.
-template <bool ANY_HIT, bool STATS>
+// any_hit: stop at the first hit (shadow rays); a run-time flag so one kernel can trace both kinds.
+template <bool STATS>
 NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
-                     bool& stack_overflow, TraceStats* stats, int postpone_pct) {
+                     bool& stack_overflow, TraceStats* stats, int postpone_pct, bool any_hit) {
 #if NGI_WHILE_WHILE
     if (postpone_pct <= 0) {
         // node phase: every lane without triangles visits nodes until all lanes hold triangles or
@@ -279,7 +280,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                 s.hu = u;
                 s.hv = v;
                 s.hit = (int)ti;
-                if (ANY_HIT) return true;
+                if (any_hit) return true;
             }
         }
         if (s.ngroup.y <= 0x00FFFFFFu) {
@@ -337,7 +338,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
             s.hu = u;
             s.hv = v;
             s.hit = (int)ti;
-            if (ANY_HIT) return true;
+            if (any_hit) return true;
         }
     }
     if (s.ngroup.y <= 0x00FFFFFFu) {
@@ -360,7 +361,7 @@ NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__
     TravState s;
     trav_init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
     uint2 stack[kTraversalStack];
-    while (!trav_step<ANY_HIT, STATS>(s, stack, nodes, tris, stack_overflow, stats, 0)) {
+    while (!trav_step<STATS>(s, stack, nodes, tris, stack_overflow, stats, 0, ANY_HIT)) {
     }
     if (s.hit >= 0) {
         tmax = s.tmax;

@@ -1157,23 +1157,28 @@ NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
 // the warp fetches that many new rays with one atomic and the lanes start them while the
 // others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
 // and removes the tail of a fixed grid.
-template <typename R, bool SHADOW, bool STATS, bool ADJ = false, bool BATCH = false>
+// KIND 0 traces the extension queue (closest hit), 1 the shadow queue (any hit), 2 both in one
+// launch: extension items first, then shadow items, each lane tracing its own kind, so shadow rays
+// fill the tail of the extension work instead of a second launch.
+template <typename R, int KIND, bool STATS, bool ADJ = false, bool BATCH = false>
 __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone,
                                                       int num_prims, const JobView<R>* __restrict__ jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
     if (ADJ) adj_smem_clear(gsm, num_prims);
-    const int n = SHADOW ? w.ctr->sh_count : w.ctr->ext_count;
-    int* fetch = SHADOW ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
+    const int n_ext = KIND == 1 ? 0 : w.ctr->ext_count;
+    const int n = n_ext + (KIND == 0 ? 0 : w.ctr->sh_count);
+    int* fetch = KIND == 1 ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
     TravState s;
     uint2 stack[kTraversalStack];
     int item = -1, slot = -1, job = 0;
+    bool shadow = KIND == 1;
     const CwNode* nodes = sv.nodes;
     const float4* tris = sv.tris;
     int num_nodes = sv.num_nodes;
     bool exhausted = false;
     bool overflow = false;
-    TraceStats ts{0u, 0u};
+    TraceStats ts{0u, 0u}, ts_sh{0u, 0u};
     while (true) {
         const bool idle = item < 0;
         const unsigned idle_mask = __ballot_sync(0xFFFFFFFFu, idle);
@@ -1186,14 +1191,15 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
             if (idle) {
                 const int i = base + __popc(idle_mask & lanemask_lt());
                 if (i < n) {
-                    item = i;
+                    shadow = i >= n_ext;
+                    item = shadow ? i - n_ext : i;
                     float4 o, d;
-                    if (SHADOW) {
-                        o = w.sh_o[i];
-                        d = w.sh_d[i];
-                        if (BATCH) job = w.sh_job[i];
+                    if (shadow) {
+                        o = w.sh_o[item];
+                        d = w.sh_d[item];
+                        if (BATCH) job = w.sh_job[item];
                     } else {
-                        slot = w.ext_queue[i];
+                        slot = w.ext_queue[item];
                         o = w.ray_o[slot];
                         d = w.ray_d[slot];
                         if (BATCH) job = w.job[slot];
@@ -1211,9 +1217,9 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
         if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
         if (item >= 0) {
             const bool done = num_nodes == 0 ||
-                              trav_step<SHADOW, STATS>(s, stack, nodes, tris, overflow, &ts, postpone);
+                              trav_step<STATS>(s, stack, nodes, tris, overflow, shadow ? &ts_sh : &ts, postpone, shadow);
             if (done) {
-                if (SHADOW) {
+                if (shadow) {
                     if (s.hit < 0) {
                         const Vec4T<R> c = w.sh_c[item];
                         const V3<R> cc = v3<R>(c.x, c.y, c.z);
@@ -1246,11 +1252,19 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
     if (ADJ) adj_flush(w, gsm, num_prims);
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
     if (STATS) {
-        warp_sum_add(SHADOW ? &w.ctr->sh_nodes : &w.ctr->ext_nodes, ts.nodes);
-        warp_sum_add(SHADOW ? &w.ctr->sh_tris : &w.ctr->ext_tris, ts.tris);
+        if (KIND != 1) {
+            warp_sum_add(&w.ctr->ext_nodes, ts.nodes);
+            warp_sum_add(&w.ctr->ext_tris, ts.tris);
+        }
+        if (KIND != 0) {
+            warp_sum_add(&w.ctr->sh_nodes, ts_sh.nodes);
+            warp_sum_add(&w.ctr->sh_tris, ts_sh.tris);
+        }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        atomicAdd(SHADOW ? &w.ctr->stat_shadow : &w.ctr->stat_ext, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (KIND != 1) atomicAdd(&w.ctr->stat_ext, (unsigned long long)n_ext);
+        if (KIND != 0) atomicAdd(&w.ctr->stat_shadow, (unsigned long long)(n - n_ext));
+    }
 }
 
 // ---- parity hooks --------------------------------------------------------------------------
@@ -1578,7 +1592,17 @@ struct TraceGrids {
         static const int g = persistent_grid(k_trace<R, true, STATS, ADJ, BATCH>, kTraceBlock);
         return g;
     }
+    static int merged() {
+        static const int g = persistent_grid(k_trace<R, 2, STATS, ADJ, BATCH>, kTraceBlock);
+        return g;
+    }
 };
+
+// One traversal launch per iteration over both queues (KIND 2) instead of two: shadow rays fill
+// the extension launch's tail. Terrain: 1483 vs 1417 Mrays/s.
+#ifndef NGI_MERGED_TRACE
+#define NGI_MERGED_TRACE 1
+#endif
 
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
 void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const RenderConsts& rc, WaveCounters* ctr,
@@ -1601,12 +1625,23 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
     const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
+#if NGI_MERGED_TRACE
+    (void)g_ext;
+    (void)g_sh;
+    k_trace<R, 2, STATS, ADJ, BATCH><<<TraceGrids<R, STATS, ADJ, BATCH>::merged(), kTraceBlock, adj_bytes, stream>>>(
+        sv, v, refill, postpone, rc.num_prims, jobs);
+    if (ev) {
+        cudaEventRecord(ev[2], stream);
+        cudaEventRecord(ev[3], stream);  // no separate shadow launch: its time is inside ev[1]..ev[2]
+    }
+#else
     k_trace<R, false, STATS, false, BATCH><<<g_ext, kTraceBlock, 0, stream>>>(sv, v, refill, postpone, rc.num_prims,
                                                                              jobs);
     if (ev) cudaEventRecord(ev[2], stream);
     k_trace<R, true, STATS, ADJ, BATCH><<<g_sh, kTraceBlock, adj_bytes, stream>>>(sv, v, refill, postpone,
                                                                                  rc.num_prims, jobs);
     if (ev) cudaEventRecord(ev[3], stream);
+#endif
 }
 
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
@@ -1622,6 +1657,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
 
     TraceGrids<R, STATS, ADJ, BATCH>::ext();
     TraceGrids<R, STATS, ADJ, BATCH>::shadow();
+    TraceGrids<R, STATS, ADJ, BATCH>::merged();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
