@@ -226,7 +226,10 @@ def run_reference(args):
     from oracle.oracle import OracleScene
 
     ora = OracleScene.from_desc(desc, WIDTH / HEIGHT)
-    n_step = int(os.environ.get("NGI_REF_SAMPLES_PER_STEP", "100000"))
+    # ~2 s of work per step on 16 cores: large enough that the per-thread film set-up the reference
+    # also pays (one W x H film per thread, src/nanogi.cpp:298) does not dominate
+    default_step = {"terrain": WIDTH * HEIGHT * 4, "cornell": WIDTH * HEIGHT * 64, "interior": 2_000_000}[WORKLOAD]
+    n_step = int(os.environ.get("NGI_REF_SAMPLES_PER_STEP", str(default_step)))
     for i in range(args.warmup):
         ora.render(RENDERER, num_samples=n_step // 4, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT,
                    seed=100 + i, rng_mode="reference", grain=1000)
