@@ -337,7 +337,7 @@ def main():
     ext_bytes = st_c["extension_rays"] * (32 + 16) + 80 * st_c["extend_nodes"] + 48 * st_c["extend_tris"]
     sh_bytes = st_c["shadow_rays"] * (32 + 4) + 80 * st_c["shadow_nodes"] + 48 * st_c["shadow_tris"]
     launches = st_t["extend_launches"]
-    if st_t["shadow_ms"] < 0.01 * st_t["extend_ms"] and st_c["shadow_rays"] > 0:
+    if st_t["shadow_launches"] == 0 and st_c["shadow_rays"] > 0:
         # one traversal launch per iteration traces both queues (no separate shadow launch to time)
         kern = {"k_logic": st_t["logic_ms"], "k_trace<extension+shadow>": st_t["extend_ms"]}
         top, alg_bytes = "k_trace<extension+shadow>", ext_bytes + sh_bytes

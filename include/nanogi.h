@@ -115,7 +115,9 @@ typedef struct ngi_render_stats {
     int64_t iterations;        /* wave iterations executed */
     int64_t nonfinite;         /* NaN/Inf contributions dropped (reported, never trapped) */
     double render_ms;          /* device time of the render (CUDA events on the render stream) */
-    /* NGI_RENDER_KERNEL_TIMING: summed device time and launch count per kernel */
+    /* NGI_RENDER_KERNEL_TIMING: summed device time and launch count per kernel. When one
+     * traversal launch per iteration traces both the extension and the shadow queue (the
+     * default build), extend_* cover that launch and shadow_launches is 0. */
     double logic_ms, extend_ms, shadow_ms;
     int64_t logic_launches, extend_launches, shadow_launches;
     /* NGI_RENDER_TRAVERSAL_COUNTERS: nodes / triangles visited, over all rays of each kind */

@@ -92,7 +92,8 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 // Measured on the 1.55M-triangle terrain: 1333 Mrays/s against 1105 with one node per step;
 // the single-product box compare adds 0.7%. Measured and not kept: a speculative second
 // triangle group (lanes with triangles visiting nodes while others search; 1389 vs 1418) and a
-// folded quantised-plane form (one subtraction less per plane, boxes two quanta wider; 1010 vs 1076).
+// folded quantised-plane form (one subtraction less per plane, boxes two quanta wider; 1010 vs 1076),
+// and three-input min.f32 / max.f32 for the slab entry and exit (1631 vs 1633: no change).
 #ifndef NGI_WHILE_WHILE
 #define NGI_WHILE_WHILE 1
 #endif
@@ -123,6 +124,22 @@ NGI_D float2 plane_pair(uint32_t near_word, uint32_t far_word, int j, float2 s2,
     const float2 q = make_float2(__uint_as_float(__byte_perm(near_word, 0x4B000000u, 0x7440u + (uint32_t)j)),
                                  __uint_as_float(__byte_perm(far_word, 0x4B000000u, 0x7440u + (uint32_t)j)));
     return __ffma2_rn(__fadd2_rn(q, make_float2(-8388608.0f, -8388608.0f)), s2, a2);
+}
+
+// Hit-mask bits of four children at once from their meta bytes (SIMD within a register, as
+// in Ylitie et al. 2017, section 4): a meta byte is (child bits << 5) | slot, where an
+// internal child has slot 24..31 (bits 3 and 4 set) and its bit index is reordered by the
+// ray octant; a leaf's slot is its first triangle's offset 0..23. An empty child has meta 0
+// and so sets no bit, without a test of its own. Measured on the 1.55M-triangle terrain:
+// 1633 Mrays/s against 1559 for the per-child decode.
+#ifndef NGI_META_SWAR
+#define NGI_META_SWAR 1
+#endif
+NGI_D void meta_decode4(uint32_t meta4, uint32_t octinv4, uint32_t& bit_index4, uint32_t& child_bits4) {
+    const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+    const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;  // per byte 0x00 or 0xFF (no carries)
+    bit_index4 = (meta4 ^ (octinv4 & inner_mask4)) & 0x1F1F1F1Fu;
+    child_bits4 = (meta4 >> 5) & 0x07070707u;
 }
 
 // Per-ray state of one CWBVH traversal, kept in registers between steps so a warp can
@@ -179,9 +196,16 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
     const float az = (n0.z - s.rp.oz) * s.idz;
     const bool nx = s.dneg & 1u, ny = s.dneg & 2u, nz = s.dneg & 4u;
     uint32_t hitmask = 0;
+#if NGI_META_SWAR
+    const uint32_t octinv4 = s.octinv * 0x01010101u;
+#endif
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         const uint32_t meta4 = __float_as_uint(half == 0 ? n1.z : n1.w);
+#if NGI_META_SWAR
+        uint32_t bit_index4, child_bits4;
+        meta_decode4(meta4, octinv4, bit_index4, child_bits4);
+#endif
         const uint32_t qlx = __float_as_uint(half == 0 ? n2.x : n2.y);
         const uint32_t qly = __float_as_uint(half == 0 ? n2.z : n2.w);
         const uint32_t qlz = __float_as_uint(half == 0 ? n3.x : n3.y);
@@ -194,7 +218,6 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
         const uint32_t nearz = nz ? qhz : qlz, farz = nz ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
 #if NGI_PACKED_BOX
             const float2 px = plane_pair(nearx, farx, j, make_float2(sx, sx), make_float2(ax, ax));
             const float2 py = plane_pair(neary, fary, j, make_float2(sy, sy), make_float2(ay, ay));
@@ -208,15 +231,21 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
             const float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
             const float tf = fminf(fminf(x1, y1), fminf(z1, s.tmax));
 #if NGI_BOX_ONEMUL
-            if (m != 0u && tn <= tf * kBoxRatio) {
+            const bool box = tn <= tf * kBoxRatio;
 #else
-            if (m != 0u && tn * kBoxLo <= tf * kBoxHi) {
+            const bool box = tn * kBoxLo <= tf * kBoxHi;
 #endif
+#if NGI_META_SWAR
+            if (box) hitmask |= ((child_bits4 >> (8 * j)) & 7u) << ((bit_index4 >> (8 * j)) & 31u);
+#else
+            const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
+            if (m != 0u && box) {
                 const uint32_t child_bits = m >> 5;
                 const bool inner = (m & 0x18u) == 0x18u;
                 const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ s.octinv) : (m & 0x1Fu);
                 hitmask |= child_bits << bit_index;
             }
+#endif
         }
     }
     return hitmask;

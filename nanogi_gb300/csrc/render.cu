@@ -1732,9 +1732,17 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     cudaEventElapsedTime(&ms, wv->ev0, wv->ev1);
     const WaveCounters& c = *wv->h_ctr;
     ds.last_stats.logic_ms = kms[0];
+    ds.last_stats.logic_launches = ds.last_stats.extend_launches = launches;
+#if NGI_MERGED_TRACE
+    // one traversal launch traces both queues: its time is extend_ms, no shadow launch exists
+    ds.last_stats.extend_ms = kms[1] + kms[2];
+    ds.last_stats.shadow_ms = 0;
+    ds.last_stats.shadow_launches = 0;
+#else
     ds.last_stats.extend_ms = kms[1];
     ds.last_stats.shadow_ms = kms[2];
-    ds.last_stats.logic_launches = ds.last_stats.extend_launches = ds.last_stats.shadow_launches = launches;
+    ds.last_stats.shadow_launches = launches;
+#endif
     ds.last_stats.extend_nodes = (int64_t)c.ext_nodes;
     ds.last_stats.extend_tris = (int64_t)c.ext_tris;
     ds.last_stats.shadow_nodes = (int64_t)c.sh_nodes;
