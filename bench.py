@@ -183,14 +183,18 @@ def measured_peak():
 
 def ncu_traffic():
     """DRAM bytes as a fraction of the traversal kernel's algorithmic bytes, from the committed
-    ncu summary of the terrain workload (applied to the full-size launch), if any."""
+    ncu summaries of the terrain workload: the full-size measurement when present, else the
+    small case's (an upper bound for the full-size launch)."""
     import re
 
-    p = ROOT / "profiles" / "k_trace_terrain_small.md"
-    if WORKLOAD == "terrain" and p.exists():
-        m = re.search(r"^dram_fraction_of_algorithmic:\s*([0-9.]+)", p.read_text(), re.M)
-        if m:
-            return float(m.group(1))
+    if WORKLOAD != "terrain":
+        return None
+    for name in ("k_trace_terrain_dram_1080p.md", "k_trace_terrain_small.md"):
+        p = ROOT / "profiles" / name
+        if p.exists():
+            m = re.search(r"^dram_fraction_of_algorithmic:\s*([0-9.]+)", p.read_text(), re.M)
+            if m:
+                return float(m.group(1))
     return None
 
 

@@ -42,6 +42,9 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 // Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
 // FP32 logic at 128 registers (25% occupancy); 4 caps it at 64 registers with ~250 B of spills
 // to L1, and was faster on the terrain (1384 vs 1322 Mrays/s): the kernel waits on HBM.
+// Also measured and not kept: 3 blocks (1579 vs 1621-1631 Mrays/s), and a bulk L2 prefetch
+// (cp.async.bulk.prefetch) of the next loop iteration's slot arrays, alone (1460-1586) or with
+// the next hit's triangle and normals (1551); the prefetched lines likely compete with the BVH for L2.
 #ifndef NGI_LOGIC_MIN_BLOCKS
 #define NGI_LOGIC_MIN_BLOCKS 4
 #endif
