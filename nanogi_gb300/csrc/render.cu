@@ -48,6 +48,9 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 #ifndef NGI_LOGIC_MIN_BLOCKS
 #define NGI_LOGIC_MIN_BLOCKS 4
 #endif
+#ifndef NGI_LOGIC_EARLY_HIT
+#define NGI_LOGIC_EARLY_HIT 0
+#endif
 #ifndef NGI_TRACE_MIN_BLOCKS
 #define NGI_TRACE_MIN_BLOCKS 8
 #endif
@@ -439,6 +442,15 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
         uint8_t st = w.state[s];
+#if NGI_LOGIC_EARLY_HIT
+        // the hit record is loaded together with the slot state, not after it: one HBM latency
+        // less on the chain hit -> triangle -> material of a slot in flight (a volatile load, so
+        // it is not moved into the branch that uses it)
+        float4 h_early;
+        asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(h_early.x), "=f"(h_early.y), "=f"(h_early.z), "=f"(h_early.w)
+                     : "l"(w.hit + s));
+#endif
         bool need_new = st == SLOT_EMPTY;
         bool want_ext = false;
         ShadowRay<R> sa;
@@ -450,7 +462,11 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
         if (st == SLOT_ACTIVE) {
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
             bool alive = false;
+#if NGI_LOGIC_EARLY_HIT
+            const float4 h = h_early;
+#else
             const float4 h = w.hit[s];
+#endif
             const int ti = __float_as_int(h.w);
             if (ti >= 0) {
                 const int job = BATCH ? w.job[s] : 0;
