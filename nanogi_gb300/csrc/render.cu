@@ -45,11 +45,10 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 // Also measured and not kept: 3 blocks (1579 vs 1621-1631 Mrays/s), and a bulk L2 prefetch
 // (cp.async.bulk.prefetch) of the next loop iteration's slot arrays, alone (1460-1586) or with
 // the next hit's triangle and normals (1551); the prefetched lines likely compete with the BVH for L2.
+// No change (1875-1880 against 1875): loading the hit record together with the slot state, and an
+// emitter cdf search in float pairs instead of FP64 (the FP64 pipe is 23% busy in this kernel).
 #ifndef NGI_LOGIC_MIN_BLOCKS
 #define NGI_LOGIC_MIN_BLOCKS 4
-#endif
-#ifndef NGI_LOGIC_EARLY_HIT
-#define NGI_LOGIC_EARLY_HIT 0
 #endif
 #ifndef NGI_TRACE_MIN_BLOCKS
 #define NGI_TRACE_MIN_BLOCKS 8
@@ -442,15 +441,6 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
         uint8_t st = w.state[s];
-#if NGI_LOGIC_EARLY_HIT
-        // the hit record is loaded together with the slot state, not after it: one HBM latency
-        // less on the chain hit -> triangle -> material of a slot in flight (a volatile load, so
-        // it is not moved into the branch that uses it)
-        float4 h_early;
-        asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];"
-                     : "=f"(h_early.x), "=f"(h_early.y), "=f"(h_early.z), "=f"(h_early.w)
-                     : "l"(w.hit + s));
-#endif
         bool need_new = st == SLOT_EMPTY;
         bool want_ext = false;
         ShadowRay<R> sa;
@@ -462,11 +452,7 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
         if (st == SLOT_ACTIVE) {
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
             bool alive = false;
-#if NGI_LOGIC_EARLY_HIT
-            const float4 h = h_early;
-#else
             const float4 h = w.hit[s];
-#endif
             const int ti = __float_as_int(h.w);
             if (ti >= 0) {
                 const int job = BATCH ? w.job[s] : 0;
