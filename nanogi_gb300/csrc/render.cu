@@ -56,13 +56,17 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 
 enum : uint8_t { SLOT_EMPTY = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
 
+// Kernels add to these with one atomic per warp (queue appends, sample claims) or per block
+// (event counts, see BlockCounts); per-thread atomics on them queued at one L2 slice and cost the
+// terrain 8% and the Cornell box a third of their throughput. Placing each counter on its own
+// 128-byte line made no difference once they were gone.
 struct WaveCounters {
     unsigned long long next_sample;   // samples claimed so far (local index)
-    int ext_count;
+    int ext_count;                    // reset before every iteration: ext_count .. sh_fetch
     int sh_count;
     int active;
-    int ext_fetch;                    // rays handed out by the persistent extension kernel
-    int sh_fetch;                     // rays handed out by the persistent shadow kernel
+    int ext_fetch;                    // rays handed out by the persistent traversal kernel
+    int sh_fetch;                     // rays handed out by the shadow-only traversal kernel
     int error_flags;                  // bit 0: traversal stack overflow
     unsigned long long stat_camera;
     unsigned long long stat_ext;
@@ -162,9 +166,37 @@ NGI_D int warp_append(int* counter, bool want) {
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
     return want ? base + __popc(mask & lanemask_lt()) : -1;
 }
-NGI_D void warp_add_u64(unsigned long long* counter, bool flag) {
-    const unsigned mask = __ballot_sync(0xFFFFFFFFu, flag);
-    if (mask != 0u && lane_id() == (unsigned)(__ffs(mask) - 1)) atomicAdd(counter, (unsigned long long)__popc(mask));
+// Adds per-thread counts (traversal statistics) into a global counter with one atomic per warp;
+// called where every lane of the warp is present.
+NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+    if (lane_id() == 0 && x) atomicAdd(counter, x);
+}
+
+// Event counts of a logic kernel's block, kept in shared memory and added to the wave's
+// counters once when the block ends.
+struct BlockCounts {
+    unsigned int active, camera, contrib, nonfinite;
+};
+NGI_D void block_counts_init(BlockCounts& b) {
+    if (threadIdx.x == 0) b = BlockCounts{0u, 0u, 0u, 0u};
+    __syncthreads();
+}
+// warp vote, one shared-memory add per warp (all lanes of the warp present)
+NGI_D void block_count_warp(unsigned int* c, bool flag) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, flag);
+    if (lane_id() == 0 && m) atomicAdd(c, (unsigned)__popc(m));
+}
+NGI_D void block_counts_flush(const BlockCounts& b, WaveCounters* ctr) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (b.active) atomicAdd(&ctr->active, (int)b.active);
+        if (b.camera) atomicAdd(&ctr->stat_camera, (unsigned long long)b.camera);
+        if (b.contrib) atomicAdd(&ctr->stat_contrib, (unsigned long long)b.contrib);
+        if (b.nonfinite) atomicAdd(&ctr->stat_nonfinite, (unsigned long long)b.nonfinite);
+    }
 }
 
 template <typename R>
@@ -438,6 +470,8 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
     float* gsm = (ADJ && !DIRECT && rc0.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
     if (ADJ && !DIRECT) adj_smem_clear(gsm, rc0.num_prims);
     const int stride = gridDim.x * blockDim.x;
+    __shared__ BlockCounts bc;
+    block_counts_init(bc);
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
         uint8_t st = w.state[s];
@@ -484,10 +518,10 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
                         if (!is_zero(c)) {
                             if (finite3(c)) {
                                 film_add(film, pixel, c);
-                                atomicAdd(&w.ctr->stat_contrib, 1ull);
+                                atomicAdd(&bc.contrib, 1u);
                                 if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim, gsm, rc.num_prims);
                             } else {
-                                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                                atomicAdd(&bc.nonfinite, 1u);
                             }
                         }
                     }
@@ -658,7 +692,7 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
                     }
                 }
             }
-            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+            block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
         }
         if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
         if (want_ext) st = SLOT_ACTIVE;
@@ -678,11 +712,9 @@ __global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R
             const int q = warp_append(&w.ctr->ext_count, want_ext);
             if (want_ext) w.ext_queue[q] = s;
         }
-        {
-            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
-            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
-        }
+        block_count_warp(&bc.active, st != SLOT_DONE);
     }
+    block_counts_flush(bc, w.ctr);  // every thread of the block ran the same iterations
     if (ADJ && !DIRECT) adj_flush(w, gsm, rc0.num_prims);
 }
 
@@ -755,6 +787,8 @@ NGI_D R light_position_pdf(const DevLight<R>& L) {
 template <typename R, bool DIRECT>
 __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
     const int stride = gridDim.x * blockDim.x;
+    __shared__ BlockCounts bc;
+    block_counts_init(bc);
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
         uint8_t st = w.state[s];
@@ -783,9 +817,9 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
                         if (!is_zero(c)) {
                             if (finite3(c)) {
                                 film_add(w.film, (uint32_t)pixel_index(g.uvx, g.uvy, rc.width, rc.height), c);
-                                atomicAdd(&w.ctr->stat_contrib, 1ull);
+                                atomicAdd(&bc.contrib, 1u);
                             } else {
-                                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                                atomicAdd(&bc.nonfinite, 1u);
                             }
                         }
                     }
@@ -880,7 +914,7 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
                     }
                 }
             }
-            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+            block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
         }
         if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
         if (want_ext) st = SLOT_ACTIVE;
@@ -898,11 +932,9 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
             const int q = warp_append(&w.ctr->ext_count, want_ext);
             if (want_ext) w.ext_queue[q] = s;
         }
-        {
-            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
-            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
-        }
+        block_count_warp(&bc.active, st != SLOT_DONE);
     }
+    block_counts_flush(bc, w.ctr);
 }
 
 // ---- bdpt (ProcessSample_BDPT, src/nanogi.cpp:1133-1194) ---------------------------------------
@@ -975,7 +1007,7 @@ NGI_D void bd_first_vertex(const SceneView<R>& sv, BdVert<R>* V, uint32_t vbase,
 // when every strategy is done; otherwise `cursor` holds the next one.
 template <typename R>
 NGI_D bool bd_connect(const SceneView<R>& sv, const RenderConsts& rc, const WaveView<R>& w, const BdVert<R>* VL,
-                      const BdVert<R>* VE, int nL, int nE, int& cursor, ShadowRay<R>* out) {
+                      const BdVert<R>* VE, int nL, int nE, int& cursor, ShadowRay<R>* out, BlockCounts& bc) {
     int emitted = 0;
     int n = cursor >> 8, s0 = cursor & 0xFF;
     for (; n <= nL + nE; n++, s0 = -1) {
@@ -999,7 +1031,7 @@ NGI_D bool bd_connect(const SceneView<R>& sv, const RenderConsts& rc, const Wave
             C = C * bd_mis_weight(sv, x) / bd_selection_prob<R>(n, s);
             if (is_zero(C)) continue;
             if (!finite3(C)) {
-                atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                atomicAdd(&bc.nonfinite, 1u);
                 continue;
             }
             // Path::RasterPosition (bdpt.hpp:204-211)
@@ -1016,7 +1048,7 @@ NGI_D bool bd_connect(const SceneView<R>& sv, const RenderConsts& rc, const Wave
                 o.light_prim = -1;
             } else {
                 film_add(w.film, pixel, C);
-                atomicAdd(&w.ctr->stat_contrib, 1ull);
+                atomicAdd(&bc.contrib, 1u);
             }
         }
     }
@@ -1032,6 +1064,8 @@ NGI_D bool bd_connect(const SceneView<R>& sv, const RenderConsts& rc, const Wave
 template <typename R>
 __global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
     const int stride = gridDim.x * blockDim.x;
+    __shared__ BlockCounts bc;
+    block_counts_init(bc);
     for (int base = blockIdx.x * blockDim.x; base < w.Q; base += stride) {
         const int s = base + (int)threadIdx.x;  // Q is a multiple of the block size
         uint8_t st = w.state[s];
@@ -1076,7 +1110,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R>
                 cursor = 2 << 8;
             }
             if (phase == 2) {
-                if (bd_connect(sv, rc, w, VL, VE, nL, nE, cursor, sh)) {
+                if (bd_connect(sv, rc, w, VL, VE, nL, nE, cursor, sh, bc)) {
                     need_new = true;
                     st = SLOT_EMPTY;
                 }
@@ -1118,7 +1152,7 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R>
                     st = SLOT_ACTIVE;
                 }
             }
-            warp_add_u64(&w.ctr->stat_camera, need_new && st != SLOT_DONE);
+            block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
         }
         w.state[s] = st;
         w.sample[s] = sample;
@@ -1138,23 +1172,14 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R>
             const int q = warp_append(&w.ctr->ext_count, want_ext);
             if (want_ext) w.ext_queue[q] = s;
         }
-        {
-            const unsigned alive = __ballot_sync(0xFFFFFFFFu, st != SLOT_DONE);
-            if (alive != 0u && lane_id() == (unsigned)(__ffs(alive) - 1)) atomicAdd(&w.ctr->active, __popc(alive));
-        }
+        block_count_warp(&bc.active, st != SLOT_DONE);
     }
+    block_counts_flush(bc, w.ctr);
 }
 
 // Which logic kernel a wave runs.
 constexpr int kLogicCamera = 0, kLogicLight = 1, kLogicBdpt = 2;
 
-// Adds a per-thread traversal count into a global counter with one atomic per warp.
-NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
-    unsigned long long x = v;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
-    if (lane_id() == 0 && x) atomicAdd(counter, x);
-}
 
 // ---- persistent traversal -------------------------------------------------------------------
 // Warps stay resident and trace until both the queue and their lanes are empty. A lane
@@ -1184,6 +1209,10 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
     bool exhausted = false;
     bool overflow = false;
     TraceStats ts{0u, 0u}, ts_sh{0u, 0u};
+    // film contributions of the block, counted in shared memory (no register kept for them)
+    __shared__ unsigned int blk_contrib;
+    if (threadIdx.x == 0) blk_contrib = 0u;
+    __syncthreads();
     while (true) {
         const bool idle = item < 0;
         const unsigned idle_mask = __ballot_sync(0xFFFFFFFFu, idle);
@@ -1231,7 +1260,7 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                         if (finite3(cc)) {
                             const uint32_t pix = w.sh_pix[item];
                             film_add(BATCH ? jobs[job].film : w.film, pix, cc);
-                            atomicAdd(&w.ctr->stat_contrib, 1ull);
+                            atomicAdd(&blk_contrib, 1u);
                             if (ADJ) {
                                 const int2 info = w.sh_info[item];
                                 const int count = info.x & 0xFF;
@@ -1244,7 +1273,7 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
                                                num_prims);
                             }
                         } else {
-                            atomicAdd(&w.ctr->stat_nonfinite, 1ull);
+                            atomicAdd(&w.ctr->stat_nonfinite, 1ull);  // rare: no register kept for it
                         }
                     }
                 } else {
@@ -1254,6 +1283,8 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
             }
         }
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && blk_contrib) atomicAdd(&w.ctr->stat_contrib, (unsigned long long)blk_contrib);
     if (ADJ) adj_flush(w, gsm, num_prims);
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
     if (STATS) {
