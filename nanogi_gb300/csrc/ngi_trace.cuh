@@ -101,9 +101,11 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 // for triangles stop, and resume after the triangle tests (0: the node phase runs until no lane
 // searches). Without it the lanes holding triangles wait for the warp's longest search. Measured
 // on the 1.55M-triangle terrain: 0: 1631, 15: 1760, 30: 1809, 40: 1821, 50: 1818, 60: 1792,
-// 75: 1719, 90: 1593 Mrays/s; on the 10M-triangle interior 440 (0) against 512 (60).
+// 75: 1719, 90: 1593 Mrays/s; on the 10M-triangle interior 440 (0) against 512 (60). With the
+// triangle-phase exit at 15 and the logic counters in shared memory: 30: 1994, 40: 2036,
+// 45: 2059, 50: 2067, 55: 2069, 60: 2061.
 #ifndef NGI_NODE_EXIT_PCT
-#define NGI_NODE_EXIT_PCT 40
+#define NGI_NODE_EXIT_PCT 50
 #endif
 // Triangle-phase exit, the same for the triangle tests: lanes with untested triangles keep them
 // (in the ray state) and finish them in the next step (0: test until every lane is done).

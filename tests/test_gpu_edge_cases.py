@@ -225,3 +225,42 @@ def test_scaled_ray_offsets_replay_the_oracle(native_lib, tmp_path, scale):
     f32 = _r(renderer="ptdirect", num_samples=n, max_num_vertices=8, width=W, height=H, seed=12,
              ray_offset="scaled").render(scene)
     assert rel_rmse(f32, unit) < 1e-3
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
+def test_instrumented_renders_count_the_same_paths(native_lib, cornell, renderer):
+    """Kernel timing and traversal counters change how a render is launched and observed, never
+    what it computes: the film and every path count match the plain render of the same samples.
+    The counts themselves are summed per block in shared memory, so they are checked against what
+    the sample count implies."""
+    from nanogi_gb300 import capi
+
+    desc, path = cornell
+    W, H, spp = 32, 32, 16
+    scene = _scene(path, W / H)
+    runs = {}
+    for flags in (0, capi.KERNEL_TIMING, capi.TRAVERSAL_COUNTERS):
+        r = _r(renderer=renderer, num_samples=W * H * spp, max_num_vertices=8, width=W, height=H, seed=7,
+               wave_size=4096, flags=flags)
+        film = r.render(scene)
+        runs[flags] = (film, dict(r.last_stats))
+    film0, st0 = runs[0]
+    assert st0["camera_rays"] == W * H * spp
+    assert st0["extension_rays"] >= st0["camera_rays"]
+    assert st0["film_contributions"] > 0
+    if renderer == "ptdirect":
+        assert st0["shadow_rays"] > 0
+    for flags, (film, st) in runs.items():
+        np.testing.assert_allclose(film, film0, rtol=1e-9, atol=1e-12)
+        # (iterations differ: graph launches run whole groups of iterations, timed runs stop at the last)
+        for k in ("camera_rays", "extension_rays", "shadow_rays", "film_contributions"):
+            assert st[k] == st0[k], (flags, k)
+    st_t = runs[capi.KERNEL_TIMING][1]
+    assert st_t["logic_launches"] == st_t["extend_launches"] == st_t["iterations"]
+    assert st_t["shadow_launches"] == 0  # one traversal launch traces both queues
+    assert st_t["logic_ms"] > 0 and st_t["extend_ms"] > 0 and st_t["shadow_ms"] == 0
+    st_c = runs[capi.TRAVERSAL_COUNTERS][1]
+    assert st_c["extend_nodes"] >= st_c["extension_rays"] > 0
+    assert st_c["extend_tris"] > 0
+    if renderer == "ptdirect":
+        assert st_c["shadow_nodes"] > 0
