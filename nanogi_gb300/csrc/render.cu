@@ -480,8 +480,16 @@ constexpr int kLogicFused = 0, kLogicShade = 1, kLogicRegen = 2;
 #ifndef NGI_SPLIT_LOGIC
 #define NGI_SPLIT_LOGIC 1
 #endif
+#ifndef NGI_SHADE_MIN_BLOCKS
+#define NGI_SHADE_MIN_BLOCKS 4
+#endif
+#ifndef NGI_REGEN_MIN_BLOCKS
+#define NGI_REGEN_MIN_BLOCKS 4
+#endif
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false, int PART = kLogicFused>
-__global__ void __launch_bounds__(256, NGI_LOGIC_MIN_BLOCKS) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
+__global__ void __launch_bounds__(256, PART == kLogicFused  ? NGI_LOGIC_MIN_BLOCKS
+                                       : PART == kLogicShade ? NGI_SHADE_MIN_BLOCKS
+                                                             : NGI_REGEN_MIN_BLOCKS) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
                                                const JobView<R>* __restrict__ jobs, int num_jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && !DIRECT && rc0.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
