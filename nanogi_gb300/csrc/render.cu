@@ -1877,7 +1877,11 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     if (p.num_samples == 0) return;
     const bool bdpt = p.renderer == NGI_RENDERER_BDPT;
     // 2^23 path slots (~0.9 GB FP32): on the terrain 1356 Mrays/s against 1322 at 2^22 and 1318
-    // at 2^24. bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): 2^18.
+    // at 2^24 (2100 against 2082 and 2025 at 2^22 / 2^21 with the current kernels). bdpt keeps
+    // 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): 2^18. A smaller default for scenes
+    // with a small BVH (2^20 below 32 MB) was measured and not kept: the Cornell box bench ran at
+    // 4995 against 4050 Mrays/s, but its convergence study took 0.253 against 0.225 s and the
+    // 256-job batch rendered one job at a time 3719 against 4431 Mrays/s.
     int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (1 << 23));
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
