@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--workload", default="terrain", choices=sorted(WORKLOADS))
     ap.add_argument("--spp-per-step", type=int, default=0, help="0 = the workload's default")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--trace-all-rays", action="store_true",
+                    help="also trace the ptdirect extension rays whose hit cannot score (as the reference does)")
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -292,9 +294,12 @@ def main():
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
+    base_flags = capi.TRACE_ALL_RAYS if args.trace_all_rays else 0
+
     def render_step(offset, flags=0):
         r = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
-                        height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision, flags=flags,
+                        height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision,
+                        flags=flags | base_flags,
                         wave_size=args.wave_size, trace_refill=args.trace_refill,
                         trace_postpone=args.trace_postpone, iterations_per_graph=args.iterations_per_graph)
         r.render_device(scene, film.data_ptr(), stream.cuda_stream)
@@ -371,7 +376,7 @@ def main():
     r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
                         height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size,
                         trace_refill=args.trace_refill, trace_postpone=args.trace_postpone,
-                        iterations_per_graph=args.iterations_per_graph)
+                        iterations_per_graph=args.iterations_per_graph, flags=base_flags)
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0
@@ -398,7 +403,10 @@ def main():
                                    f"{RENDERER}, max length {MAX_VERTICES}, {spp} spp per step",
                        "spp_total": spp * args.steps,
                        "precision": f"{args.precision} shading, fp64 film", "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{world}, disjoint sample ranges"},
+                       "parallelism": f"replicas x{world}, disjoint sample ranges",
+                       "rays": ("every ray the reference traces" if args.trace_all_rays or RENDERER != "ptdirect" else
+                                "traced rays; ptdirect extension rays whose hit Russian roulette ends are not traced "
+                                "(same film; --trace-all-rays traces them)")},
             "msamples_per_s": all_samples / (ms / 1e3) / 1e6,
             "rays_per_sample": all_rays / max(all_samples, 1),
             "bvh_build_ms": info["bvh_build_ms"], "bvh_bytes": info["bvh_bytes"],

@@ -101,10 +101,16 @@ typedef enum ngi_ray_offset {
     NGI_RAY_OFFSET_SCALED = 1
 } ngi_ray_offset;
 
-/* Measurement flags (results in ngi_render_stats). Both change only how the render is
- * launched or instrumented, never its result. */
+/* Render flags. The first two are measurement flags (results in ngi_render_stats); none of the
+ * three changes the film. */
 #define NGI_RENDER_KERNEL_TIMING 1        /* launch without graphs, CUDA events around each kernel */
 #define NGI_RENDER_TRAVERSAL_COUNTERS 2   /* count BVH nodes and triangles visited per ray */
+/* ptdirect scores only through next-event estimation at vertices that survive Russian roulette,
+ * and the roulette variable of a path's next hit is drawn with its current vertex: by default an
+ * extension ray whose hit the roulette (or the length limit) will end is not traced. The film is
+ * the same sample for sample; extension_rays counts the rays traced. This flag traces them all,
+ * as the reference does (ray counts then match the reference's). */
+#define NGI_RENDER_TRACE_ALL_RAYS 4
 
 /* Counters of the last render on a scene handle (per-stage ray counts etc). */
 typedef struct ngi_render_stats {

@@ -51,6 +51,7 @@ class RenderParams(ctypes.Structure):
 
 KERNEL_TIMING = 1
 TRAVERSAL_COUNTERS = 2
+TRACE_ALL_RAYS = 4
 
 
 class RenderStats(ctypes.Structure):

@@ -246,7 +246,11 @@ def test_instrumented_renders_count_the_same_paths(native_lib, cornell, renderer
         runs[flags] = (film, dict(r.last_stats))
     film0, st0 = runs[0]
     assert st0["camera_rays"] == W * H * spp
-    assert st0["extension_rays"] >= st0["camera_rays"]
+    if renderer == "pt":
+        assert st0["extension_rays"] >= st0["camera_rays"]
+    else:
+        # ptdirect does not trace toward a hit that Russian roulette or the length limit ends
+        assert 0 < st0["extension_rays"] < st0["camera_rays"]
     assert st0["film_contributions"] > 0
     if renderer == "ptdirect":
         assert st0["shadow_rays"] > 0
@@ -264,3 +268,27 @@ def test_instrumented_renders_count_the_same_paths(native_lib, cornell, renderer
     assert st_c["extend_tris"] > 0
     if renderer == "ptdirect":
         assert st_c["shadow_nodes"] > 0
+
+
+def test_ptdirect_untraced_dead_rays_leave_the_film_unchanged(native_lib, cornell):
+    """Skipping the extension rays whose hit Russian roulette or the length limit ends changes the
+    rays traced, never the film: the default render equals the one that traces every ray."""
+    from nanogi_gb300 import capi
+
+    desc, path = cornell
+    W, H, spp = 24, 24, 32
+    scene = _scene(path, W / H)
+    films, stats = [], []
+    for flags in (0, capi.TRACE_ALL_RAYS):
+        for m in (8, 3):
+            r = _r(renderer="ptdirect", num_samples=W * H * spp, max_num_vertices=m, width=W, height=H, seed=11,
+                   wave_size=8192, flags=flags)
+            films.append(r.render(scene))
+            stats.append(dict(r.last_stats))
+    for k in range(2):
+        np.testing.assert_allclose(films[k], films[k + 2], rtol=1e-9, atol=1e-12)
+        assert stats[k]["film_contributions"] == stats[k + 2]["film_contributions"]
+        assert stats[k]["shadow_rays"] == stats[k + 2]["shadow_rays"]
+        assert stats[k]["extension_rays"] < stats[k + 2]["extension_rays"]
+    # with every ray traced, each sample traces its camera ray
+    assert stats[2]["extension_rays"] >= W * H * spp
