@@ -105,9 +105,9 @@ typedef enum ngi_ray_offset {
  * three changes the film. */
 #define NGI_RENDER_KERNEL_TIMING 1        /* launch without graphs, CUDA events around each kernel */
 #define NGI_RENDER_TRAVERSAL_COUNTERS 2   /* count BVH nodes and triangles visited per ray */
-/* ptdirect scores only through next-event estimation at vertices that survive Russian roulette,
- * and the roulette variable of a path's next hit is drawn with its current vertex: by default an
- * extension ray whose hit the roulette (or the length limit) will end is not traced. The film is
+/* ptdirect and ltdirect score only through connections made at vertices that survive Russian
+ * roulette, and the roulette variable of a path's next hit is drawn with its current vertex: by
+ * default an extension ray whose hit the roulette (or the length limit) will end is not traced. The film is
  * the same sample for sample; extension_rays counts the rays traced. This flag traces them all,
  * as the reference does (ray counts then match the reference's). */
 #define NGI_RENDER_TRACE_ALL_RAYS 4

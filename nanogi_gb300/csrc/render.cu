@@ -474,7 +474,7 @@ NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const Wav
 
 // ptdirect scores only through next-event estimation, which a vertex does after it survives
 // Russian roulette (src/nanogi.cpp:646-785: NEE at the loop top, the roulette right after the
-// intersection). The roulette variable of the next hit is the .w of the Philox call this vertex
+// intersection); ltdirect likewise only through its sensor connections (src/nanogi.cpp:955-1130). The roulette variable of the next hit is the .w of the Philox call this vertex
 // already drew for its own next-event estimation, so a path that the roulette -- or the length
 // limit -- ends at its next hit gains nothing from that hit: its extension ray is not traced.
 // The film is the same, sample for sample; fewer rays are traced per sample (terrain: 0.93
@@ -893,15 +893,17 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
                     if (!(rc.max_vertices != -1 && nv >= rc.max_vertices) && mat.bsdf != BSDF_NONE) {
                         tangent_space(g);
                         const V3<R> wi = -d;
+                        bool dead = false;
                         if (DIRECT) {
                             const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
                             const R pdf_pe = light_position_pdf(sv.lights[w.pixel[s]]);
                             sensor_connect(sv, rc, g, (const DevLight<R>*)nullptr, &mat, wi, thr, pdf_pe, un, sa);
+                            dead = next_hit_is_dead(rc, un.w, nv);  // ltdirect scores only by connections
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
                         V3<R> wo, wgt;
-                        if (bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y, (R)ud.z,
-                                               wo, wgt, true)) {
+                        if (!dead && bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y,
+                                                        (R)ud.z, wo, wgt, true)) {
                             thr = thr * wgt;
                             store_ray(w, s, g, wo, rc.ray_offset);
                             w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
@@ -954,14 +956,16 @@ __global__ void __launch_bounds__(256) k_logic_lt(SceneView<R> sv, WaveView<R> w
                     sample_light_position(sv, L, (R)ul.x, (R)ul.y, gl);
                     const R pdf_pl = light_position_pdf(L);
                     V3<R> thr = v3<R>(1, 1, 1) / pdf_pl / (R(1) / (R)nl);  // pdfL = 1 / #lights
+                    bool dead = false;
                     if (DIRECT) {
                         const float4 un = rng4(rk, 1u, RNG_NEE_RR);
                         sensor_connect(sv, rc, gl, &L, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, pdf_pl, un,
                                        sb);
+                        dead = next_hit_is_dead(rc, un.w, 1);
                     }
                     const float4 ud = rng4(rk, 1u, RNG_DIR);
                     V3<R> wo, wgt;
-                    if (light_sample_direction(L, gl, (R)ud.x, (R)ud.y, wo, wgt)) {
+                    if (!dead && light_sample_direction(L, gl, (R)ud.x, (R)ud.y, wo, wgt)) {
                         thr = thr * wgt;
                         store_ray(w, s, gl, wo, rc.ray_offset);
                         w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
