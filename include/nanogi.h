@@ -196,6 +196,12 @@ NGI_API ngi_status ngi_scene_get_triangles(const ngi_scene* scene, float* pos, f
  * by the first render/intersect; explicit so its cost can be measured apart. */
 NGI_API ngi_status ngi_scene_build(ngi_scene* scene);
 
+/* Frees the render buffers a scene handle keeps between renders (its wave of path slots and
+ * queues, up to ~2 GB); the scene itself stays on the device and the next render allocates them
+ * again. For programs that keep many scene handles alive. Not in the reference (its per-thread
+ * contexts live for one render, nanogi.cpp:281-319). */
+NGI_API ngi_status ngi_scene_release_buffers(ngi_scene* scene);
+
 /* ---- rendering --------------------------------------------------------------------- */
 
 /* Renderer::Render(const Scene&, std::vector<glm::dvec3>& film)  src/nanogi.cpp:182-221

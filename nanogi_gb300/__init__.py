@@ -109,6 +109,10 @@ class Scene:
     def build(self) -> None:
         check(load_library().ngi_scene_build(self.handle))
 
+    def release_buffers(self) -> None:
+        """Frees the render buffers kept between renders; the next render allocates them again."""
+        check(load_library().ngi_scene_release_buffers(self.handle))
+
     def intersect(self, rays: np.ndarray):
         """rays: (n, 8) float32 = ox, oy, oz, tmin, dx, dy, dz, tmax -> (prim, t, uv)."""
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)

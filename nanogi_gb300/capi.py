@@ -143,6 +143,7 @@ PROTOTYPES = {
     "ngi_scene_get_triangles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p]),
     "ngi_scene_build": (ctypes.c_int, [ctypes.c_void_p]),
+    "ngi_scene_release_buffers": (ctypes.c_int, [ctypes.c_void_p]),
     "ngi_render": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p]),
     "ngi_render_device": (ctypes.c_int, [ctypes.c_void_p, _P(RenderParams), ctypes.c_void_p, ctypes.c_void_p]),
     "ngi_get_render_stats": (ctypes.c_int, [ctypes.c_void_p, _P(RenderStats)]),

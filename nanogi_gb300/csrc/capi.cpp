@@ -197,6 +197,14 @@ NGI_API ngi_status ngi_scene_build(ngi_scene* scene) {
     });
 }
 
+NGI_API ngi_status ngi_scene_release_buffers(ngi_scene* scene) {
+    if (!scene || !scene->host) return Fail(NGI_ERR_INVALID_ARGUMENT, "scene is NULL");
+    return Guard([&]() {
+        ngi::DeviceReleaseBuffers(*scene->host);
+        return NGI_OK;
+    });
+}
+
 NGI_API ngi_status ngi_render(ngi_scene* scene, const ngi_render_params* params, double* film_rgb) {
     const ngi_status st = CheckParams(scene, params);
     if (st != NGI_OK) return st;

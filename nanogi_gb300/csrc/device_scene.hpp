@@ -68,6 +68,7 @@ struct DeviceScene {
 // Uploads the flattened scene and builds the BVH on the current device.
 void DeviceUpload(HostScene& scene);
 void DeviceFree(HostScene& scene);
+void DeviceReleaseBuffers(HostScene& scene);  // the cached wave of path slots
 void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const float* d_uv, const int* d_tri_prim,
               int n, cudaStream_t stream);
 

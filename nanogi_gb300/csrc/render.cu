@@ -1637,6 +1637,14 @@ void DeviceUpload(HostScene& hs) {
     }
 }
 
+void DeviceReleaseBuffers(HostScene& hs) {
+    DeviceScene* ds = hs.dev;
+    if (!ds) return;
+    if (ds->stream) cudaStreamSynchronize(ds->stream);
+    free_wave(ds->wave);
+    ds->wave = nullptr;
+}
+
 void DeviceFree(HostScene& hs) {
     DeviceScene* ds = hs.dev;
     if (!ds) return;
@@ -1693,7 +1701,7 @@ void alloc_wave_view(RenderWave* wv, WaveView<R>& v, int Q) {
     v.carry_out = v.carry_out_count = nullptr;
 }
 
-RenderWave* ensure_wave(DeviceScene& ds, int Q, int precision) {
+RenderWave* ensure_wave_exact(DeviceScene& ds, int Q, int precision) {
     if (ds.wave && ds.wave->Q == Q && ds.wave->precision == precision) return ds.wave;
     free_wave(ds.wave);
     ds.wave = nullptr;
@@ -1716,6 +1724,21 @@ RenderWave* ensure_wave(DeviceScene& ds, int Q, int precision) {
     }
     ds.wave = wv;
     return wv;
+}
+
+// The wave of a render, kept by the scene handle for its next render. When the device cannot hold
+// Q slots (other handles keep their own waves), the wave shrinks by halves down to 2^16 slots:
+// slower, but the render completes. The caller reads the slot count back from the wave.
+RenderWave* ensure_wave(DeviceScene& ds, int Q, int precision) {
+    while (true) {
+        try {
+            return ensure_wave_exact(ds, Q, precision);
+        } catch (const DeviceError& e) {
+            if (e.code != NGI_ERR_OUT_OF_MEMORY || Q <= (1 << 16)) throw;
+            cudaGetLastError();  // clear the allocation error
+            Q = std::max(1 << 16, (Q / 2 + 255) / 256 * 256);
+        }
+    }
 }
 
 int grid_for(int items, int block) {

@@ -260,11 +260,13 @@ def batch(num_jobs: int = 256):
     batch_wall = time.perf_counter() - t0
     rays = st["extension_rays"] + st["shadow_rays"]
     seq_ms, seq_rays = 0.0, 0
+    scenes[0].release_buffers()  # the batch's wave
     t0 = time.perf_counter()
     for sc, r in work:
         r.render(sc)
         seq_ms += r.last_stats["render_ms"]
         seq_rays += r.last_stats["extension_rays"] + r.last_stats["shadow_rays"]
+        sc.release_buffers()  # 256 handles would otherwise keep 256 waves
     seq_wall = time.perf_counter() - t0
     out = {"workload": f"{num_jobs} jobs, res {{64,128,256,512}}^2, tris log-U[1k,200k] "
                        f"(mean {np.mean([j['triangles'] for j in jobs]):.0f}), spp log-U[16,1024], max length U[4,24], ptdirect",

@@ -294,3 +294,16 @@ def test_untraced_dead_rays_leave_the_film_unchanged(native_lib, cornell, render
     if renderer == "ptdirect":
         # with every ray traced, each sample traces its camera ray
         assert stats[2]["extension_rays"] >= W * H * spp
+
+
+def test_release_buffers_between_renders(native_lib, cornell):
+    """A handle that released its render buffers renders the same film again (it allocates anew)."""
+    desc, path = cornell
+    W, H = 16, 16
+    scene = _scene(path, W / H)
+    r = _r(renderer="ptdirect", num_samples=W * H * 16, max_num_vertices=6, width=W, height=H, seed=5)
+    a = r.render(scene)
+    scene.release_buffers()
+    scene.release_buffers()  # releasing twice is harmless
+    b = r.render(scene)
+    np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12)
