@@ -78,6 +78,46 @@ NGI_D bool tri_intersect(const RayPre& r, float4 p0, float4 p1, float4 p2, float
 }
 
 constexpr int kTraversalStack = 64;
+// Shared-memory part of the traversal stack: the bottom NGI_SMEM_STACK entries of every lane's
+// stack live in shared memory, entry-major (entry i of lane t at [i * kStackLanes + t], so a
+// warp's 32 lanes touch 32 consecutive 8-byte words), and deeper entries in local memory. The
+// compressed 8-wide tree of a few million triangles rarely stacks more than 8 node groups.
+// Measured on the 1.55M-triangle terrain (Mrays/s, two runs each): 0 (all local) 1813, 4: 1794,
+// 8: 1796, 16: 1794; Cornell box 4027 (0) against 3957 (8). The local stack stays in L1, and the
+// shared-memory carve-out takes L1 capacity from the node fetches, so 0 is the default.
+#ifndef NGI_SMEM_STACK
+#define NGI_SMEM_STACK 0
+#endif
+constexpr int kStackLanes = 128;  // threads of a block that own a shared-memory stack column
+
+// One lane's traversal stack: entries below SH in its shared-memory column, the rest in local
+// memory (loc holds kTraversalStack entries; its first SH are unused when SH > 0).
+// The shared column is held as a 32-bit shared-window address (one register, not a 64-bit
+// generic pointer: the traversal runs at its 64-register cap).
+template <int SH>
+struct LaneStack {
+    uint2* loc;
+    uint32_t sh;
+    NGI_D void put(int i, uint2 v) const {
+        if (SH > 0 && i < SH)
+            asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(sh + (uint32_t)i * (kStackLanes * 8u)), "r"(v.x),
+                         "r"(v.y)
+                         : "memory");
+        else
+            loc[i] = v;
+    }
+    NGI_D uint2 get(int i) const {
+        if (SH > 0 && i < SH) {
+            uint2 v;
+            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                         : "=r"(v.x), "=r"(v.y)
+                         : "r"(sh + (uint32_t)i * (kStackLanes * 8u))
+                         : "memory");
+            return v;
+        }
+        return loc[i];
+    }
+};
 // Relative padding of the box interval: keeps the box test conservative against the few
 // ulps of rounding in the slab distances (Ize, JCGT 2013).
 constexpr float kBoxLo = 1.0f - 1.0f / 1048576.0f;
@@ -283,8 +323,8 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
 // when the ray is finished (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is
 // set, and the ray abandoned, if the tree is deeper than the stack.
 // any_hit: stop at the first hit (shadow rays); a run-time flag so one kernel can trace both kinds.
-template <bool STATS>
-NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
+template <bool STATS, int SH>
+NGI_D bool trav_step(TravState& s, LaneStack<SH> stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
                      bool& stack_overflow, TraceStats* stats, int postpone_pct, bool any_hit) {
 #if NGI_WHILE_WHILE
     if (postpone_pct <= 0) {
@@ -318,7 +358,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                         s.sp = 0;
                         continue;
                     }
-                    stack[s.sp++] = s.ngroup;
+                    stack.put(s.sp++, s.ngroup);
                 }
                 const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
                 const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
@@ -328,7 +368,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                 if (STATS) stats->nodes++;
                 s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
                 tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
-                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
+                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack.get(--s.sp);
             }
         }
 #if NGI_TRI_EXIT_PCT > 0
@@ -371,7 +411,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
 #endif
         if (s.ngroup.y <= 0x00FFFFFFu) {
             if (s.sp == 0) return true;
-            s.ngroup = stack[--s.sp];
+            s.ngroup = stack.get(--s.sp);
         }
         return false;
     }
@@ -387,7 +427,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
                 s.hit = -1;
                 return true;
             }
-            stack[s.sp++] = s.ngroup;
+            stack.put(s.sp++, s.ngroup);
         }
         const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
         const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
@@ -407,7 +447,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
         const unsigned tri_lanes = __ballot_sync(act, has_tri);
         const bool more = s.ngroup.y > 0x00FFFFFFu || s.sp > 0;
         if (has_tri && more && s.sp < kTraversalStack - 1 && __popc(tri_lanes) * 100 < __popc(act) * postpone_pct) {
-            stack[s.sp++] = tgroup;
+            stack.put(s.sp++, tgroup);
             tgroup.y = 0u;
         }
     }
@@ -429,7 +469,7 @@ NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ node
     }
     if (s.ngroup.y <= 0x00FFFFFFu) {
         if (s.sp == 0) return true;
-        s.ngroup = stack[--s.sp];
+        s.ngroup = stack.get(--s.sp);
     }
     return false;
 }
@@ -447,7 +487,8 @@ NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__
     TravState s;
     trav_init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
     uint2 stack[kTraversalStack];
-    while (!trav_step<STATS>(s, stack, nodes, tris, stack_overflow, stats, 0, ANY_HIT)) {
+    const LaneStack<0> ls{stack, 0u};
+    while (!trav_step<STATS, 0>(s, ls, nodes, tris, stack_overflow, stats, 0, ANY_HIT)) {
     }
     if (s.hit >= 0) {
         tmax = s.tmax;

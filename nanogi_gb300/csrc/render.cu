@@ -38,7 +38,9 @@ namespace ngi {
 
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 
-// Minimum resident blocks per SM asked of the traversal kernels (register budget).
+// Minimum resident blocks per SM asked of the traversal kernels (register budget). 8 blocks of
+// 128 give 64 registers and no spills. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
+// each): 8: 1809, 6 (80 registers): 1723, 10 (51, 132 B of spills): 1739, 12 (42): 1617.
 // Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
 // FP32 logic at 128 registers (25% occupancy); 4 caps it at 64 registers with ~250 B of spills
 // to L1, and was faster on the terrain (1384 vs 1322 Mrays/s): the kernel waits on HBM.
@@ -1316,6 +1318,12 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
     int* fetch = KIND == 1 ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
     TravState s;
     uint2 stack[kTraversalStack];
+#if NGI_SMEM_STACK > 0
+    __shared__ uint2 sh_stack[NGI_SMEM_STACK * kStackLanes];
+    const LaneStack<NGI_SMEM_STACK> ls{stack, (uint32_t)__cvta_generic_to_shared(sh_stack + threadIdx.x)};
+#else
+    const LaneStack<0> ls{stack, 0u};
+#endif
     int item = -1, slot = -1, job = 0;
     bool shadow = KIND == 1;
     const CwNode* nodes = sv.nodes;
@@ -1366,7 +1374,8 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
         if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
         if (item >= 0) {
             const bool done = num_nodes == 0 ||
-                              trav_step<STATS>(s, stack, nodes, tris, overflow, shadow ? &ts_sh : &ts, postpone, shadow);
+                              trav_step<STATS, NGI_SMEM_STACK>(s, ls, nodes, tris, overflow, shadow ? &ts_sh : &ts, postpone,
+                                                              shadow);
             if (done) {
                 if (shadow) {
                     if (s.hit < 0) {
@@ -1760,6 +1769,7 @@ int persistent_grid(K kernel, int block) {
 }
 
 constexpr int kTraceBlock = 128;
+static_assert(kTraceBlock == kStackLanes, "one shared-memory stack column per traversal thread");
 constexpr int kRefillLanes = 8;
 
 // Grid sizes of the persistent traversal kernels (queried once, outside any graph capture).

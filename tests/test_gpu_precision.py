@@ -75,3 +75,27 @@ def test_offset_modes_agree_under_the_reflector(native_lib, tmp_path):
     a = ng.Renderer(ray_offset="scaled", **kw).render(scene)
     b = ng.Renderer(ray_offset="reference", **kw).render(scene)
     assert a.sum() > 0 and abs(a.sum() / b.sum() - 1) < 1e-3
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
+def test_fp32_within_one_percent_of_a_64k_spp_fp64_render(native_lib, cornell, renderer):
+    """The image bar of the tuned path: on the Cornell box (max path length 8, as the 256x256
+    workload), the FP32 render differs from a 65,536-spp FP64 render by less than 1% rel-RMSE.
+    Both are rendered at 65,536 spp with independent seeds, so the figure holds the noise of
+    both films; half their squared difference estimates one film's noise, and the FP32 film's
+    bias (what remains after that noise is taken out) is held below 0.5%."""
+    import nanogi_gb300 as ng
+
+    _, path = cornell
+    W = H = 64
+    scene = ng.Scene.load(path, W / H)
+    kw = dict(renderer=renderer, num_samples=W * H * 65536, max_num_vertices=8, width=W, height=H)
+    ref = ng.Renderer(seed=101, precision="fp64", **kw).render(scene)
+    f32 = ng.Renderer(seed=202, precision="fp32", **kw).render(scene)
+    f64 = ng.Renderer(seed=303, precision="fp64", **kw).render(scene)
+    scene.close()
+    err = rel_rmse(f32, ref)
+    noise = rel_rmse(f64, ref)  # two FP64 films: the same figure with no precision difference
+    assert err < 0.01, (renderer, err, noise)
+    bias2 = max(err * err - noise * noise, 0.0)
+    assert np.sqrt(bias2) < 0.005, (renderer, err, noise)
