@@ -1758,9 +1758,25 @@ int grid_for(int items, int block) {
     return std::max(1, std::min(max_blocks, (items + block - 1) / block));
 }
 
+// Preferred shared-memory carve-out (percent of each SM's unified L1 / shared storage) of the
+// traversal and the path-logic kernels; -1 leaves the driver's choice. The driver still gives a
+// kernel the shared memory it needs. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
+// each): driver's choice 1809, traversal at 0 (largest L1) 1768, logic at 0 1810, both 1768.
+#ifndef NGI_TRACE_CARVEOUT
+#define NGI_TRACE_CARVEOUT -1
+#endif
+#ifndef NGI_LOGIC_CARVEOUT
+#define NGI_LOGIC_CARVEOUT -1
+#endif
+template <typename K>
+void set_carveout(K kernel, int pct) {
+    if (pct >= 0) CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+}
+
 // Blocks of a persistent kernel that fit on the device at once.
 template <typename K>
 int persistent_grid(K kernel, int block) {
+    set_carveout(kernel, NGI_TRACE_CARVEOUT);
     int dev = 0, sms = 152, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1894,6 +1910,26 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
 #endif
 }
 
+// Carve-out of the camera path-logic kernels a wave launches (once, before any graph capture).
+template <typename R, bool DIRECT, bool ADJ, bool BATCH, int LOGIC>
+void logic_carveout() {
+    if constexpr (NGI_LOGIC_CARVEOUT >= 0 && LOGIC == kLogicCamera) {
+        static const bool once = [] {
+            if constexpr (compact_shading<DIRECT, BATCH, LOGIC>()) {
+                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicShadeQ>, NGI_LOGIC_CARVEOUT);
+                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen>, NGI_LOGIC_CARVEOUT);
+            } else if constexpr (NGI_SPLIT_LOGIC && DIRECT && !BATCH) {
+                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicShade>, NGI_LOGIC_CARVEOUT);
+                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen>, NGI_LOGIC_CARVEOUT);
+            } else {
+                set_carveout(k_logic<R, DIRECT, ADJ, BATCH>, NGI_LOGIC_CARVEOUT);
+            }
+            return true;
+        }();
+        (void)once;
+    }
+}
+
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
 void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
               bool kernel_timing, cudaStream_t stream, const JobView<R>* jobs = nullptr, int num_jobs = 0) {
@@ -1914,6 +1950,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     TraceGrids<R, STATS, ADJ, BATCH>::ext();
     TraceGrids<R, STATS, ADJ, BATCH>::shadow();
     TraceGrids<R, STATS, ADJ, BATCH>::merged();
+    logic_carveout<R, DIRECT, ADJ, BATCH, LOGIC>();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
