@@ -231,7 +231,8 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
  *   - the scene must already be on the device (ngi_scene_build), else NGI_ERR_INVALID_ARGUMENT;
  *   - params->wave_size must be 0 (= 65536) or at most 65536 path slots, else
  *     NGI_ERR_INVALID_ARGUMENT; num_samples is not bounded (samples stream through the wave);
- *   - params->flags must be 0;
+ *   - params->flags may hold NGI_RENDER_TRACE_ALL_RAYS and nothing else (the measurement
+ *     flags need buffers of their own), else NGI_ERR_INVALID_ARGUMENT;
  *   - the caller passes the output: d_film_rgb, a DEVICE array of width*height*3 doubles that
  *     receives the raw sums added to its contents, as with ngi_render_device;
  *   - the first call on each device looks up the array's device address (with that device

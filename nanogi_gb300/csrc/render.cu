@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -2664,12 +2665,15 @@ size_t carve_wave(unsigned char* base, int Q, WaveView<R>& v) {
     return off;
 }
 
-// Device address of the scratch array, looked up once per device with that device current.
+// Device address of the scratch array, looked up once per device with that device current
+// (under a lock: host threads may make their first calls at the same time).
 unsigned char* noalloc_scratch_address() {
     static unsigned char* addr[64] = {nullptr};
+    static std::mutex lock;
     int dev = 0;
     CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) throw DeviceError("device ordinal out of range", NGI_ERR_INVALID_ARGUMENT);
+    std::lock_guard<std::mutex> guard(lock);
     if (!addr[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
