@@ -523,6 +523,53 @@ constexpr size_t kShadowPerSlot = 1 + (kRegenAttempts > 1 ? kRegenAttempts : 1);
 #ifndef NGI_REGEN_MIN_BLOCKS
 #define NGI_REGEN_MIN_BLOCKS 4
 #endif
+// Shading in class order: the queued-slot shading kernel sorts each block's items by what their
+// shading does (the BSDF of the hit primitive, a miss, a slot left empty) with a counting sort in
+// shared memory, so that the lanes of a warp take the same branches. Measured on the
+// 1.55M-triangle terrain (Mrays/s, two runs each): 1798-1802 sorted against 1803-1804, the
+// logic's share of GPU time unchanged at 36%: the shading warps do not diverge on the material
+// type. Off by default.
+#ifndef NGI_SHADE_SORT
+#define NGI_SHADE_SORT 0
+#endif
+constexpr int kShadeClasses = 8;
+
+// Item this thread shades after the block's counting sort (a permutation of the block's items;
+// items past n_items stay past it). Every thread of the block must call it.
+template <typename R>
+NGI_D int shade_sort_item(const SceneView<R>& sv, const WaveView<R>& w, int item, int n_items, int n_ext_in) {
+    __shared__ int sort_base[kShadeClasses];
+    __shared__ int sort_item[kLogicBlock];
+    int cls = kShadeClasses - 1;  // empty slot or past the end
+    if (item < n_items && item < n_ext_in) {
+        const int ti = __float_as_int(w.hit[w.ext_in[item]].w);
+        if (ti < 0) {
+            cls = kShadeClasses - 2;
+        } else {
+            const DevMaterial<R>& m = sv.mats[__float_as_int(sv.nrm[3 * (size_t)ti].w)];
+            cls = m.bsdf == BSDF_D ? 0 : m.bsdf == BSDF_G ? 1 : m.bsdf == BSDF_S ? 2 + min(max(m.s_type, 0), 2) : 5;
+        }
+    }
+    if (threadIdx.x < kShadeClasses) sort_base[threadIdx.x] = 0;
+    __syncthreads();
+    const int rank = atomicAdd(&sort_base[cls], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int c = 0; c < kShadeClasses; c++) {
+            const int n = sort_base[c];
+            sort_base[c] = acc;
+            acc += n;
+        }
+    }
+    __syncthreads();
+    sort_item[sort_base[cls] + rank] = item;
+    __syncthreads();
+    const int sorted = sort_item[threadIdx.x];
+    __syncthreads();  // the arrays are reused by the block's next round of items
+    return sorted;
+}
+
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false, int PART = kLogicFused>
 __global__ void __launch_bounds__(256, PART == kLogicFused                          ? NGI_LOGIC_MIN_BLOCKS
                                        : (PART == kLogicShade || PART == kLogicShadeQ) ? NGI_SHADE_MIN_BLOCKS
@@ -544,7 +591,10 @@ __global__ void __launch_bounds__(256, PART == kLogicFused                      
                         : PART == kLogicShadeQ ? n_ext_in + min(*w.carry_in_count, w.Q - n_ext_in)
                                                : w.Q;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += stride) {
-        const int item = base + (int)threadIdx.x;
+        int item = base + (int)threadIdx.x;
+#if NGI_SHADE_SORT
+        if constexpr (PART == kLogicShadeQ) item = shade_sort_item(sv0, w, item, n_items, n_ext_in);
+#endif
         const bool valid = item < n_items;  // false only past the end of a queue
         int s = item;
         uint8_t st;
