@@ -39,9 +39,6 @@ namespace ngi {
 
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 
-// Minimum resident blocks per SM asked of the traversal kernels (register budget). 8 blocks of
-// 128 give 64 registers and no spills. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
-// each): 8: 1809, 6 (80 registers): 1723, 10 (51, 132 B of spills): 1739, 12 (42): 1617.
 // Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
 // FP32 logic at 128 registers (25% occupancy); 4 caps it at 64 registers with ~250 B of spills
 // to L1, and was faster on the terrain (1384 vs 1322 Mrays/s): the kernel waits on HBM.
@@ -53,6 +50,9 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 #ifndef NGI_LOGIC_MIN_BLOCKS
 #define NGI_LOGIC_MIN_BLOCKS 4
 #endif
+// Minimum resident blocks per SM asked of the traversal kernels (register budget). 8 blocks of
+// 128 give 64 registers and no spills. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
+// each): 8: 1809, 6 (80 registers): 1723, 10 (51, 132 B of spills): 1739, 12 (42): 1617.
 #ifndef NGI_TRACE_MIN_BLOCKS
 #define NGI_TRACE_MIN_BLOCKS 8
 #endif
