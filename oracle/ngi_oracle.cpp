@@ -816,7 +816,7 @@ struct RenderCtx {
     const ora_scene* s;
     const ora_render_params* p;
     std::vector<double>* film;
-    int64_t cam = 0, ext = 0, sh = 0;
+    int64_t cam = 0, ext = 0, sh = 0, miss = 0;
     long long strat_end = 0;
 };
 
@@ -926,7 +926,10 @@ void ProcessSample(RenderCtx& c, Sampler& smp) {
         c.ext++;
         float tmin;
         const dv3 ro = RayOrigin(geom, wo, P.ray_offset, tmin);
-        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) break;
+        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) {
+            c.miss++;
+            break;
+        }
         const Prim& hp = s.prims[is.prim];
         if (!direct && (hp.d.type & L)) {
             const dv3 Le = EvaluateDirection(hp, is.geom, L, dv3(), -wo, false, false);
@@ -1021,7 +1024,10 @@ void ProcessSampleLT(RenderCtx& c, Sampler& smp) {
         c.ext++;
         float tmin;
         const dv3 ro = RayOrigin(geom, wo, P.ray_offset, tmin);
-        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) break;
+        if (!Intersect(s, bvh, ro, wo, is, tmin, InfF, P.ray_offset)) {
+            c.miss++;
+            break;
+        }
         const Prim& hp = s.prims[is.prim];
         if (!direct && (hp.d.type & E)) {
             // Hit with the sensor (src/nanogi.cpp:871-896)
@@ -1104,7 +1110,10 @@ void SampleSubpath(RenderCtx& c, Sampler& smp, bool le, uint32_t vbase, std::vec
         c.ext++;
         float tmin;
         const dv3 ro = RayOrigin(pv.geom, wo, P.ray_offset, tmin);
-        if (!Intersect(s, P.use_bvh != 0, ro, wo, is, tmin, InfF, P.ray_offset)) break;
+        if (!Intersect(s, P.use_bvh != 0, ro, wo, is, tmin, InfF, P.ray_offset)) {
+            c.miss++;
+            break;
+        }
         PVert v;
         v.geom = is.geom;
         v.prim = &s.prims[is.prim];
@@ -1459,6 +1468,7 @@ int ora_render(ora_scene* s, const ora_render_params* p, double* film_out, ora_r
             stats->camera_rays += c.cam;
             stats->extension_rays += c.ext;
             stats->shadow_rays += c.sh;
+            stats->extension_misses += c.miss;
         }
         stats->seconds = std::chrono::duration<double>(t1 - t0).count();
         stats->threads = threads;

@@ -69,6 +69,7 @@ typedef struct ora_render_stats {
     int64_t camera_rays, extension_rays, shadow_rays;
     double seconds;
     int32_t threads;
+    int64_t extension_misses;  /* extension rays (camera rays included) that hit nothing */
 } ora_render_stats;
 
 typedef struct ora_scene ora_scene;

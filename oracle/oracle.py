@@ -62,7 +62,8 @@ class RenderParams(ctypes.Structure):
 
 class RenderStats(ctypes.Structure):
     _fields_ = [("camera_rays", ctypes.c_int64), ("extension_rays", ctypes.c_int64),
-                ("shadow_rays", ctypes.c_int64), ("seconds", ctypes.c_double), ("threads", ctypes.c_int32)]
+                ("shadow_rays", ctypes.c_int64), ("seconds", ctypes.c_double), ("threads", ctypes.c_int32),
+                ("extension_misses", ctypes.c_int64)]
 
 
 _lib = None
