@@ -82,7 +82,6 @@ def parse():
     ap.add_argument("--scene-dir", default=None)
     ap.add_argument("--wave-size", type=int, default=0, help="path slots (0 = library default)")
     ap.add_argument("--trace-refill", type=int, default=0, help="traversal refill threshold (0 = default)")
-    ap.add_argument("--trace-postpone", type=int, default=0, help="triangle postponing, percent + 1 (0 = default)")
     ap.add_argument("--iterations-per-graph", type=int, default=0, help="wave iterations per CUDA graph (0 = default)")
     args = ap.parse_args()
     configure(args)
@@ -301,7 +300,7 @@ def main():
                         height=HEIGHT, seed=1234 + rank, sample_offset=offset, precision=args.precision,
                         flags=flags | base_flags,
                         wave_size=args.wave_size, trace_refill=args.trace_refill,
-                        trace_postpone=args.trace_postpone, iterations_per_graph=args.iterations_per_graph)
+                        iterations_per_graph=args.iterations_per_graph)
         r.render_device(scene, film.data_ptr(), stream.cuda_stream)
         return r.last_stats
 
@@ -375,8 +374,8 @@ def main():
     host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
     r_e2e = ng.Renderer(renderer=RENDERER, num_samples=n_step, max_num_vertices=MAX_VERTICES, width=WIDTH,
                         height=HEIGHT, seed=99 + rank, precision=args.precision, wave_size=args.wave_size,
-                        trace_refill=args.trace_refill, trace_postpone=args.trace_postpone,
-                        iterations_per_graph=args.iterations_per_graph, flags=base_flags)
+                        trace_refill=args.trace_refill, iterations_per_graph=args.iterations_per_graph,
+                        flags=base_flags)
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0

@@ -47,7 +47,7 @@ typedef enum ngi_status {
     NGI_ERR_NO_DEVICE = 8         /* no CUDA device visible */
 } ngi_status;
 
-/* Renderer names of the reference (src/nanogi.cpp:51-69); only the path tracers are built. */
+/* Renderer names of the reference (src/nanogi.cpp:51-69). All five estimators are built; ptmnee is not. */
 typedef enum ngi_renderer_type {
     NGI_RENDERER_PT = 0,       /* "pt"       : ProcessSample_PT       src/nanogi.cpp:446-607 */
     NGI_RENDERER_PTDIRECT = 1, /* "ptdirect" : ProcessSample_PTDirect src/nanogi.cpp:609-802 */
@@ -87,8 +87,7 @@ typedef struct ngi_render_params {
     int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
     int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
     int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
-    int32_t trace_postpone;    /* triangle tests wait while fewer than (value-1)% of a warp's lanes have
-                                  some (1..101, 1 = never wait); 0 = auto */
+    int32_t reserved;          /* must be 0 */
     int32_t ray_offset;        /* ngi_ray_offset: how rays leave a surface */
 } ngi_render_params;
 
@@ -121,9 +120,9 @@ typedef struct ngi_render_stats {
     int64_t iterations;        /* wave iterations executed */
     int64_t nonfinite;         /* NaN/Inf contributions dropped (reported, never trapped) */
     double render_ms;          /* device time of the render (CUDA events on the render stream) */
-    /* NGI_RENDER_KERNEL_TIMING: summed device time and launch count per kernel. When one
-     * traversal launch per iteration traces both the extension and the shadow queue (the
-     * default build), extend_* cover that launch and shadow_launches is 0. */
+    /* NGI_RENDER_KERNEL_TIMING: summed device time and launch count per kernel. One traversal
+     * launch per iteration traces both the extension and the shadow queue: extend_* cover that
+     * launch, and shadow_ms / shadow_launches are 0. */
     double logic_ms, extend_ms, shadow_ms;
     int64_t logic_launches, extend_launches, shadow_launches;
     /* NGI_RENDER_TRAVERSAL_COUNTERS: nodes / triangles visited, over all rays of each kind */
@@ -225,18 +224,27 @@ NGI_API ngi_status ngi_get_render_stats(const ngi_scene* scene, ngi_render_stats
  * synchronisation cudaMalloc / cudaFree may cause, or a process held to a fixed memory
  * budget. The call allocates nothing (no cudaMalloc, cudaFree, graph or event creation):
  * the render's scratch -- its wave of path slots, queues and counters -- lives in one
- * 32 MiB file-scope device array that every GPU loading this library holds until exit.
+ * 32 MiB file-scope device array.
  *
  * Limits and rules:
- *   - the scene must already be on the device (ngi_scene_build), else NGI_ERR_INVALID_ARGUMENT;
+ *   - pt and ptdirect only; lt, ltdirect and bdpt return NGI_ERR_UNSUPPORTED;
+ *   - the scene must already be on the device (ngi_scene_build), else NGI_ERR_INVALID_ARGUMENT,
+ *     and that device must be the current one, else NGI_ERR_INVALID_ARGUMENT;
  *   - params->wave_size must be 0 (= 65536) or at most 65536 path slots, else
  *     NGI_ERR_INVALID_ARGUMENT; num_samples is not bounded (samples stream through the wave);
  *   - params->flags may hold NGI_RENDER_TRACE_ALL_RAYS and nothing else (the measurement
  *     flags need buffers of their own), else NGI_ERR_INVALID_ARGUMENT;
+ *   - params->iterations_per_graph sets how many wave iterations run between two reads of the
+ *     wave's counters (0 = 4; odd counts are rounded up to even);
  *   - the caller passes the output: d_film_rgb, a DEVICE array of width*height*3 doubles that
  *     receives the raw sums added to its contents, as with ngi_render_device;
- *   - the first call on each device looks up the array's device address (with that device
- *     current); make that first call before any stream capture;
+ *   - the 32 MiB are reserved on a device the first time this library's render code runs
+ *     there (CUDA loads it lazily) and are held until the process exits. A caller whose own
+ *     allocator will take the whole device makes one call first, before that allocator starts:
+ *     a call with num_samples = 0 does this set-up (and looks up the array's device address)
+ *     without rendering;
+ *   - every call reads the wave's counters back to the host and synchronises the stream, so it
+ *     cannot be made while the stream is being captured into a CUDA graph;
  *   - every call shares the array and clears what must start at zero; calls that overlap on
  *     the GPU (e.g. from two streams at once) race on it and must not be made. */
 NGI_API ngi_status ngi_render_device_noalloc(ngi_scene* scene, const ngi_render_params* params,

@@ -168,13 +168,12 @@ class Renderer:
     iterations_per_graph: int = 0
     flags: int = 0
     trace_refill: int = 0
-    trace_postpone: int = 0
     ray_offset: str = "reference"
     last_stats: dict = field(default_factory=dict, repr=False)
 
     def params(self) -> RenderParams:
         if self.renderer not in capi.RENDERERS:
-            raise NanogiError(1, f"renderer '{self.renderer}' is not built (pt, ptdirect)")
+            raise NanogiError(1, f"renderer '{self.renderer}' is not one of pt, ptdirect, lt, ltdirect, bdpt")
         return RenderParams(
             renderer=capi.RENDERERS[self.renderer],
             max_num_vertices=int(self.max_num_vertices),
@@ -189,7 +188,6 @@ class Renderer:
             iterations_per_graph=int(self.iterations_per_graph),
             flags=int(self.flags),
             trace_refill=int(self.trace_refill),
-            trace_postpone=int(self.trace_postpone),
             ray_offset=capi.RAY_OFFSETS[self.ray_offset],
         )
 

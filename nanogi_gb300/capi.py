@@ -44,7 +44,7 @@ class RenderParams(ctypes.Structure):
         ("iterations_per_graph", ctypes.c_int32),
         ("flags", ctypes.c_int32),
         ("trace_refill", ctypes.c_int32),
-        ("trace_postpone", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("ray_offset", ctypes.c_int32),
     ]
 

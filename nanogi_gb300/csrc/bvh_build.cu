@@ -4,14 +4,12 @@
 //   1. per-triangle bounds and centroid bounds
 //   2. 63-bit Morton codes of the centroids, radix sort (CUB)
 //   3. binary tree: PLOC clustering of the sorted leaves (Meister and Bittner 2018), leaves
-//      renumbered depth-first so every subtree is a contiguous range; or, with NGI_BVH_PLOC=0,
-//      the binary radix tree (Karras, HPG 2012) and a bottom-up bounds refit
+//      renumbered depth-first so every subtree is a contiguous range
 //   4. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017): a
 //      bottom-up pass finds the SAH-optimal way to write every subtree as at most 1..8
-//      roots, and each node opens its binary descendants as that minimum says (with
-//      NGI_BVH_DP_COLLAPSE=0: greedily by largest area); subtrees of <= 3 triangles become
-//      leaves, children are assigned to slots by ray octant, and child boxes are quantised
-//      to 8 bits per plane relative to the parent.
+//      roots, and each node opens its binary descendants as that minimum says; subtrees of
+//      <= 3 triangles become leaves, children are assigned to slots by ray octant, and child
+//      boxes are quantised to 8 bits per plane relative to the parent.
 //   5. triangles, normals and uvs are gathered into leaf order.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
@@ -114,78 +112,6 @@ __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict
     }
     keys[i] = (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
     vals[i] = (uint32_t)i;
-}
-
-__device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, int64_t n, int64_t i, int64_t j) {
-    if (j < 0 || j >= n) return -1;
-    const uint64_t a = keys[i], b = keys[j];
-    if (a == b) return 64 + __clz((uint32_t)i ^ (uint32_t)j);
-    return __clzll(a ^ b);
-}
-
-// Karras 2012: internal node i covers sorted range [first, last], split after gamma.
-__global__ void k_radix_tree(const uint64_t* __restrict__ keys, int n, uint32_t* __restrict__ left,
-                             uint32_t* __restrict__ right, int* __restrict__ int_parent,
-                             int* __restrict__ leaf_parent, int2* __restrict__ range) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-    const int dmin = delta(keys, n, i, i - d);
-    int64_t lmax = 2;
-    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
-    int64_t l = 0;
-    for (int64_t t = lmax / 2; t >= 1; t /= 2)
-        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
-    const int64_t j = i + l * d;
-    const int dnode = delta(keys, n, i, j);
-    int64_t s = 0, t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
-    } while (t > 1);
-    const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
-    const int64_t first = d > 0 ? i : j, last = d > 0 ? j : i;
-    uint32_t lref, rref;
-    if (first == gamma) { lref = kLeafFlag | (uint32_t)gamma; leaf_parent[gamma] = (int)i; }
-    else { lref = (uint32_t)gamma; int_parent[gamma] = (int)i; }
-    if (last == gamma + 1) { rref = kLeafFlag | (uint32_t)(gamma + 1); leaf_parent[gamma + 1] = (int)i; }
-    else { rref = (uint32_t)(gamma + 1); int_parent[gamma + 1] = (int)i; }
-    left[i] = lref;
-    right[i] = rref;
-    range[i] = make_int2((int)first, (int)last);
-    if (i == 0) int_parent[0] = -1;
-}
-
-__device__ __forceinline__ float4 ld_cg(const float4* p) { return __ldcg(p); }
-
-// Bottom-up bounds: the second thread to reach a node computes it.
-__global__ void k_refit(int n, const uint32_t* __restrict__ sorted_tri, const float4* __restrict__ tlo,
-                        const float4* __restrict__ thi, const uint32_t* __restrict__ left,
-                        const uint32_t* __restrict__ right, const int* __restrict__ int_parent,
-                        const int* __restrict__ leaf_parent, float4* leaf_lo, float4* leaf_hi, float4* int_lo,
-                        float4* int_hi, int* __restrict__ arrivals, int* __restrict__ error_flag) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const uint32_t tri = sorted_tri[j];
-    leaf_lo[j] = tlo[tri];
-    leaf_hi[j] = thi[tri];
-    __threadfence();
-    int p = leaf_parent[j];
-    // A radix tree over 63-bit keys with 32-bit index tie-breaks is at most ~96 levels deep.
-    for (int steps = 0; p >= 0; steps++) {
-        if (steps > 256) { atomicOr(error_flag, 1); return; }
-        if (atomicAdd(&arrivals[p], 1) == 0) return;
-        __threadfence();
-        const uint32_t l = left[p], r = right[p];
-        const float4 a_lo = (l & kLeafFlag) ? ld_cg(&leaf_lo[l & ~kLeafFlag]) : ld_cg(&int_lo[l]);
-        const float4 a_hi = (l & kLeafFlag) ? ld_cg(&leaf_hi[l & ~kLeafFlag]) : ld_cg(&int_hi[l]);
-        const float4 b_lo = (r & kLeafFlag) ? ld_cg(&leaf_lo[r & ~kLeafFlag]) : ld_cg(&int_lo[r]);
-        const float4 b_hi = (r & kLeafFlag) ? ld_cg(&leaf_hi[r & ~kLeafFlag]) : ld_cg(&int_hi[r]);
-        __stcg(&int_lo[p], make_float4(fminf(a_lo.x, b_lo.x), fminf(a_lo.y, b_lo.y), fminf(a_lo.z, b_lo.z), 0.0f));
-        __stcg(&int_hi[p], make_float4(fmaxf(a_hi.x, b_hi.x), fmaxf(a_hi.y, b_hi.y), fmaxf(a_hi.z, b_hi.z), 0.0f));
-        __threadfence();
-        p = int_parent[p];
-    }
 }
 
 // ---- PLOC: parallel locally-ordered clustering (Meister and Bittner, TVCG 2018) --------------
@@ -410,17 +336,10 @@ struct WorkItem {
 // 8-wide node exactly as the minimum says. With kCostNode >= 3 kCostTri a subtree of at most
 // 3 triangles is always cheapest as one leaf, so the emit step's rule (internal iff more than
 // 3 triangles) matches every choice the minimum makes. Measured on the 1.55M-triangle terrain
-// against the greedy collapse below: 11.96 nodes and 3.99 triangles per ray instead of 12.51
-// and 4.66, 1631 Mrays/s against 1563 (kCostTri 0.2: 1628).
-
-#ifndef NGI_BVH_DP_COLLAPSE
-#define NGI_BVH_DP_COLLAPSE 1
-#endif
-#ifndef NGI_BVH_COST_TRI
-#define NGI_BVH_COST_TRI 0.3f
-#endif
+// against a greedy collapse (open the child of largest area until 8): 11.96 nodes and 3.99
+// triangles per ray instead of 12.51 and 4.66, 1631 Mrays/s against 1563 (kCostTri 0.2: 1628).
 constexpr float kCostNode = 1.0f;
-constexpr float kCostTri = NGI_BVH_COST_TRI;
+constexpr float kCostTri = 0.3f;
 static_assert(kCostNode >= kLeafMax * kCostTri, "a leaf of <= kLeafMax triangles must never cost more than a node");
 
 // Per internal node: cost[2p], cost[2p+1] hold C(p, 1..8); split[p] byte i-1 (i >= 2) holds the
@@ -529,29 +448,8 @@ __global__ void k_collapse_plan(BinView b, const WorkItem* __restrict__ work, in
     const uint32_t ref = work[w].ref;
     uint32_t ch[8];
     int nc = 0;
-    if (ref & kLeafFlag) {
-        ch[nc++] = ref;
-    } else if (split != nullptr) {
-        nc = dp_children(b, split, ref, ch);
-    } else {
-        ch[nc++] = b.left[ref];
-        ch[nc++] = b.right[ref];
-        while (nc < 8) {
-            int best = -1;
-            float best_area = -1.0f;
-            for (int c = 0; c < nc; c++) {
-                if ((ch[c] & kLeafFlag) || ref_count(b, ch[c]) <= kLeafMax) continue;
-                float4 lo, hi;
-                ref_bounds(b, ch[c], lo, hi);
-                const float a = half_area(lo, hi);
-                if (a > best_area) { best_area = a; best = c; }
-            }
-            if (best < 0) break;
-            const uint32_t open = ch[best];
-            ch[best] = b.left[open];
-            ch[nc++] = b.right[open];
-        }
-    }
+    if (ref & kLeafFlag) ch[nc++] = ref;
+    else nc = dp_children(b, split, ref, ch);
     int ni = 0, nt = 0;
     for (int c = 0; c < 8; c++) {
         uint32_t r = c < nc ? ch[c] : 0xFFFFFFFFu;
@@ -714,17 +612,12 @@ T* dev_alloc(size_t count, std::vector<void*>& temps) {
 
 }  // namespace
 
-// PLOC against the radix tree of the same Morton keys: terrain 1322 vs 1305 Mrays/s (12.5 nodes
-// and 4.7 triangles per ray against 12.1 and 4.8); the 10M-triangle interior halves its work per
-// ray (30 nodes and 15 triangles against 55 and 30). Build: 8 ms for 1.55M triangles, 20 ms for 10M.
-#ifndef NGI_BVH_PLOC
-#define NGI_BVH_PLOC 1
-#endif
-constexpr bool kUsePloc = NGI_BVH_PLOC != 0;
-
 // PLOC binary tree over the Morton-sorted leaves, then depth-first leaf positions so that every
-// subtree is a contiguous range (what the 8-wide collapse reads). Fills the same arrays as the
-// radix tree + refit path and returns the root's reference. leaf_tri receives the triangle of
+// subtree is a contiguous range (what the 8-wide collapse reads); returns the root's reference.
+// Measured against the binary radix tree of the same Morton keys (Karras, HPG 2012) with a
+// bottom-up refit: terrain 1322 vs 1305 Mrays/s (12.5 nodes and 4.7 triangles per ray against
+// 12.1 and 4.8); the 10M-triangle interior halves its work per ray (30 nodes and 15 triangles
+// against 55 and 30). Build: 8 ms for 1.55M triangles, 20 ms for 10M. leaf_tri receives the triangle of
 // each depth-first leaf position.
 uint32_t BuildPloc(int n, const uint32_t* sorted_tri, const float4* tlo, const float4* thi, uint32_t* left,
                    uint32_t* right, int* int_parent, int* leaf_parent, int2* range, float4* leaf_lo, float4* leaf_hi,
@@ -847,22 +740,13 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             uint32_t root_ref = n == 1 ? (kLeafFlag | 0u) : 0u;
             uint32_t* leaf_tri = vals_s;  // triangle of each leaf position
             if (n == 1) {
+                // a single leaf: its box is the triangle's
                 BVH_CHECK(cudaMemsetAsync(leaf_parent, 0xFF, sizeof(int), stream));  // -1
-            }
-            if (n > 1 && kUsePloc) {
+                k_leaf_gather<<<1, 32, 0, stream>>>(1, vals_s, tlo, thi, leaf_lo, leaf_hi, left);
+                BVH_CHECK(cudaGetLastError());
+            } else {
                 root_ref = BuildPloc(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, range, leaf_lo, leaf_hi,
                                      int_lo, int_hi, arrivals, leaf_tri, temps, stream);
-            } else {
-                if (n > 1)
-                    k_radix_tree<<<(n - 1 + T - 1) / T, T, 0, stream>>>(keys_s, n, left, right, int_parent, leaf_parent,
-                                                                     range);
-                k_refit<<<nb, T, 0, stream>>>(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, leaf_lo,
-                                             leaf_hi, int_lo, int_hi, arrivals, arrivals + ni);
-                BVH_CHECK(cudaGetLastError());
-                int refit_err = 0;
-                BVH_CHECK(cudaMemcpyAsync(&refit_err, arrivals + ni, sizeof(int), cudaMemcpyDeviceToHost, stream));
-                BVH_CHECK(cudaStreamSynchronize(stream));
-                if (refit_err) throw DeviceError("BVH refit walked past the maximum tree depth");
             }
 
             // 8-wide collapse, one level per iteration.
@@ -888,7 +772,7 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             BVH_CHECK(cudaMemcpyAsync(work_a, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
             BinView bv{left, right, range, leaf_lo, leaf_hi, int_lo, int_hi};
             uint2* split = nullptr;
-            if (NGI_BVH_DP_COLLAPSE && n > 1) {
+            if (n > 1) {
                 float4* cost = dev_alloc<float4>(2 * (size_t)ni, temps);
                 split = dev_alloc<uint2>(ni, temps);
                 BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));

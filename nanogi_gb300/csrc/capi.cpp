@@ -72,8 +72,7 @@ ngi_status CheckParams(const ngi_scene* scene, const ngi_render_params* p) {
         return Fail(NGI_ERR_INVALID_ARGUMENT, "wave_size / iterations_per_graph out of range");
     if (p->trace_refill < 0 || p->trace_refill > 32)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_refill must be 0 (auto) or 1..32");
-    if (p->trace_postpone < 0 || p->trace_postpone > 101)
-        return Fail(NGI_ERR_INVALID_ARGUMENT, "trace_postpone must be 0 (auto) or 1..101");
+    if (p->reserved != 0) return Fail(NGI_ERR_INVALID_ARGUMENT, "the reserved field must be 0");
     if (p->ray_offset != NGI_RAY_OFFSET_REFERENCE && p->ray_offset != NGI_RAY_OFFSET_SCALED)
         return Fail(NGI_ERR_INVALID_ARGUMENT, "ray_offset must be REFERENCE or SCALED");
     return NGI_OK;

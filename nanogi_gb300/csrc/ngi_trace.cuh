@@ -78,65 +78,28 @@ NGI_D bool tri_intersect(const RayPre& r, float4 p0, float4 p1, float4 p2, float
 }
 
 constexpr int kTraversalStack = 64;
-// Shared-memory part of the traversal stack: the bottom NGI_SMEM_STACK entries of every lane's
-// stack live in shared memory, entry-major (entry i of lane t at [i * kStackLanes + t], so a
-// warp's 32 lanes touch 32 consecutive 8-byte words), and deeper entries in local memory. The
-// compressed 8-wide tree of a few million triangles rarely stacks more than 8 node groups.
-// Measured on the 1.55M-triangle terrain (Mrays/s, two runs each): 0 (all local) 1813, 4: 1794,
-// 8: 1796, 16: 1794; Cornell box 4027 (0) against 3957 (8). The local stack stays in L1, and the
-// shared-memory carve-out takes L1 capacity from the node fetches, so 0 is the default.
-#ifndef NGI_SMEM_STACK
-#define NGI_SMEM_STACK 0
-#endif
-constexpr int kStackLanes = 128;  // threads of a block that own a shared-memory stack column
+// Each lane's stack of node groups (64 entries of 8 bytes) lives in local memory, which L1
+// caches. Measured and not kept: the bottom 4, 8 or 16 entries of every lane in shared memory,
+// entry-major, the rest local (Ylitie et al. 2017): 1794, 1796 and 1794 Mrays/s on the
+// 1.55M-triangle terrain against 1813 all-local, and 3957 against 4027 on the Cornell box. The
+// shared-memory carve-out takes L1 capacity from the node fetches, while the local stack's few
+// hot lines per lane already hit L1.
 
-// One lane's traversal stack: entries below SH in its shared-memory column, the rest in local
-// memory (loc holds kTraversalStack entries; its first SH are unused when SH > 0).
-// The shared column is held as a 32-bit shared-window address (one register, not a 64-bit
-// generic pointer: the traversal runs at its 64-register cap).
-template <int SH>
-struct LaneStack {
-    uint2* loc;
-    uint32_t sh;
-    NGI_D void put(int i, uint2 v) const {
-        if (SH > 0 && i < SH)
-            asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(sh + (uint32_t)i * (kStackLanes * 8u)), "r"(v.x),
-                         "r"(v.y)
-                         : "memory");
-        else
-            loc[i] = v;
-    }
-    NGI_D uint2 get(int i) const {
-        if (SH > 0 && i < SH) {
-            uint2 v;
-            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                         : "=r"(v.x), "=r"(v.y)
-                         : "r"(sh + (uint32_t)i * (kStackLanes * 8u))
-                         : "memory");
-            return v;
-        }
-        return loc[i];
-    }
-};
 // Relative padding of the box interval: keeps the box test conservative against the few
 // ulps of rounding in the slab distances (Ize, JCGT 2013).
 constexpr float kBoxLo = 1.0f - 1.0f / 1048576.0f;
 constexpr float kBoxHi = 1.0f + 1.0f / 1048576.0f;
-// tn Lo <= tf Hi as one product, tn <= tf (Hi / Lo): the same test for either sign of tn and tf.
+// tn Lo <= tf Hi as one product, tn <= tf (Hi / Lo): the same test for either sign of tn and tf
+// (0.7% over two products).
 constexpr float kBoxRatio = kBoxHi / kBoxLo;
-#ifndef NGI_BOX_ONEMUL
-#define NGI_BOX_ONEMUL 1
-#endif
-// Node phase "while-while" (Aila and Laine 2009): a lane holding triangles waits while the
-// other lanes of its warp keep visiting nodes, so the triangle tests of a warp run together.
-// Measured on the 1.55M-triangle terrain: 1333 Mrays/s against 1105 with one node per step;
-// the single-product box compare adds 0.7%. Measured and not kept: a speculative second
-// triangle group (lanes with triangles visiting nodes while others search; 1389 vs 1418) and a
-// folded quantised-plane form (one subtraction less per plane, boxes two quanta wider; 1010 vs 1076),
-// and three-input min.f32 / max.f32 for the slab entry and exit (1631 vs 1633: no change).
-#ifndef NGI_WHILE_WHILE
-#define NGI_WHILE_WHILE 1
-#endif
+// The node phase is "while-while" (Aila and Laine 2009): a lane holding triangles waits while
+// the other lanes of its warp keep visiting nodes, so the triangle tests of a warp run together.
+// Measured on the 1.55M-triangle terrain: 1333 Mrays/s against 1105 with one node per step.
+// Measured and not kept: triangle postponing (Ylitie et al. 2017; slower at every threshold), a
+// speculative second triangle group (lanes with triangles visiting nodes while others search;
+// 1389 vs 1418), a folded quantised-plane form (one subtraction less per plane, boxes two quanta
+// wider; 1010 vs 1076), and three-input min.f32 / max.f32 for the slab entry and exit (1631 vs
+// 1633: no change).
 // Node-phase exit: percentage of a warp's tracing lanes below which the lanes still searching
 // for triangles stop, and resume after the triangle tests (0: the node phase runs until no lane
 // searches). Without it the lanes holding triangles wait for the warp's longest search. Measured
@@ -144,38 +107,25 @@ constexpr float kBoxRatio = kBoxHi / kBoxLo;
 // 75: 1719, 90: 1593 Mrays/s; on the 10M-triangle interior 440 (0) against 512 (60). With the
 // triangle-phase exit at 15 and the logic counters in shared memory: 30: 1994, 40: 2036,
 // 45: 2059, 50: 2067, 55: 2069, 60: 2061.
-#ifndef NGI_NODE_EXIT_PCT
-#define NGI_NODE_EXIT_PCT 50
-#endif
+constexpr int kNodeExitPct = 50;
 // Triangle-phase exit, the same for the triangle tests: lanes with untested triangles keep them
 // (in the ray state) and finish them in the next step (0: test until every lane is done).
 // Measured with the node-phase exit at 40: terrain 0: 1820, 10: 1888, 15: 1884, 20: 1870,
 // 25: 1860, 35: 1812, 50: 1710 Mrays/s; the triangle-heavy 10M-triangle interior (18 triangles
 // per ray) loses a little: 512 (0), 493 (10), 497 (15), 499 (20).
-#ifndef NGI_TRI_EXIT_PCT
-#define NGI_TRI_EXIT_PCT 15
-#endif
+constexpr int kTriExitPct = 15;
 
 struct TraceStats {
     uint32_t nodes;
     uint32_t tris;
 };
 
-// Byte b of a 32-bit word as an exact float: one byte permute builds the bit pattern of
-// 2^23 + byte, one subtraction removes the 2^23.
-NGI_D float byte_to_float(uint32_t word, int b) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u + (uint32_t)b)) - 8388608.0f;
-}
-
 // Packed box test: the near and far plane of an axis are decoded and scaled as one float2
 // through the two-wide FADD2 / FFMA2 instructions of sm_100+. Measured on the 1.55M-triangle
 // terrain: 1090 Mrays/s against 1060 for the scalar form. (Pairing the watertight triangle
 // test's multiplies and subtractions the same way gained nothing and did not reproduce the
 // scalar roundings, so that test stays scalar.)
-#ifndef NGI_PACKED_BOX
-#define NGI_PACKED_BOX 1
-#endif
-
+//
 // (near, far) plane distances of one axis for child j: (q * s + a) for the two quantised
 // bytes, q = byte - 2^23 after the permute builds 2^23 + byte.
 NGI_D float2 plane_pair(uint32_t near_word, uint32_t far_word, int j, float2 s2, float2 a2) {
@@ -190,9 +140,6 @@ NGI_D float2 plane_pair(uint32_t near_word, uint32_t far_word, int j, float2 s2,
 // ray octant; a leaf's slot is its first triangle's offset 0..23. An empty child has meta 0
 // and so sets no bit, without a test of its own. Measured on the 1.55M-triangle terrain:
 // 1633 Mrays/s against 1559 for the per-child decode.
-#ifndef NGI_META_SWAR
-#define NGI_META_SWAR 1
-#endif
 NGI_D void meta_decode4(uint32_t meta4, uint32_t octinv4, uint32_t& bit_index4, uint32_t& child_bits4) {
     const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
     const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xFFu;  // per byte 0x00 or 0xFF (no carries)
@@ -211,9 +158,7 @@ struct TravState {
     float hu, hv;
     int hit;
     uint2 ngroup;              // node group: child base, internal-hit bits [31:24] | imask [7:0]
-#if NGI_TRI_EXIT_PCT > 0
     uint2 tgroup;              // triangle group left untested by the last step
-#endif
     int sp;
 };
 
@@ -232,9 +177,7 @@ NGI_D void trav_init(TravState& s, float ox, float oy, float oz, float dx, float
     s.hu = s.hv = 0.0f;
     s.hit = -1;
     s.ngroup = make_uint2(0u, 0x80000000u);  // the root as the only internal hit, imask 0
-#if NGI_TRI_EXIT_PCT > 0
     s.tgroup = make_uint2(0u, 0u);
-#endif
     s.sp = 0;
 }
 
@@ -260,16 +203,12 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
     const float az = (n0.z - s.rp.oz) * s.idz;
     const bool nx = s.dneg & 1u, ny = s.dneg & 2u, nz = s.dneg & 4u;
     uint32_t hitmask = 0;
-#if NGI_META_SWAR
     const uint32_t octinv4 = s.octinv * 0x01010101u;
-#endif
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         const uint32_t meta4 = __float_as_uint(half == 0 ? n1.z : n1.w);
-#if NGI_META_SWAR
         uint32_t bit_index4, child_bits4;
         meta_decode4(meta4, octinv4, bit_index4, child_bits4);
-#endif
         const uint32_t qlx = __float_as_uint(half == 0 ? n2.x : n2.y);
         const uint32_t qly = __float_as_uint(half == 0 ? n2.z : n2.w);
         const uint32_t qlz = __float_as_uint(half == 0 ? n3.x : n3.y);
@@ -282,179 +221,71 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
         const uint32_t nearz = nz ? qhz : qlz, farz = nz ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-#if NGI_PACKED_BOX
             const float2 px = plane_pair(nearx, farx, j, make_float2(sx, sx), make_float2(ax, ax));
             const float2 py = plane_pair(neary, fary, j, make_float2(sy, sy), make_float2(ay, ay));
             const float2 pz = plane_pair(nearz, farz, j, make_float2(sz, sz), make_float2(az, az));
-            const float x0 = px.x, x1 = px.y, y0 = py.x, y1 = py.y, z0 = pz.x, z1 = pz.y;
-#else
-            const float x0 = fmaf(byte_to_float(nearx, j), sx, ax), x1 = fmaf(byte_to_float(farx, j), sx, ax);
-            const float y0 = fmaf(byte_to_float(neary, j), sy, ay), y1 = fmaf(byte_to_float(fary, j), sy, ay);
-            const float z0 = fmaf(byte_to_float(nearz, j), sz, az), z1 = fmaf(byte_to_float(farz, j), sz, az);
-#endif
-            const float tn = fmaxf(fmaxf(x0, y0), fmaxf(z0, s.tmin));
-            const float tf = fminf(fminf(x1, y1), fminf(z1, s.tmax));
-#if NGI_BOX_ONEMUL
-            const bool box = tn <= tf * kBoxRatio;
-#else
-            const bool box = tn * kBoxLo <= tf * kBoxHi;
-#endif
-#if NGI_META_SWAR
-            if (box) hitmask |= ((child_bits4 >> (8 * j)) & 7u) << ((bit_index4 >> (8 * j)) & 31u);
-#else
-            const uint32_t m = (meta4 >> (8 * j)) & 0xFFu;
-            if (m != 0u && box) {
-                const uint32_t child_bits = m >> 5;
-                const bool inner = (m & 0x18u) == 0x18u;
-                const uint32_t bit_index = inner ? ((m & 0x1Fu) ^ s.octinv) : (m & 0x1Fu);
-                hitmask |= child_bits << bit_index;
-            }
-#endif
+            const float tn = fmaxf(fmaxf(px.x, py.x), fmaxf(pz.x, s.tmin));
+            const float tf = fminf(fminf(px.y, py.y), fminf(pz.y, s.tmax));
+            if (tn <= tf * kBoxRatio) hitmask |= ((child_bits4 >> (8 * j)) & 7u) << ((bit_index4 >> (8 * j)) & 31u);
         }
     }
     return hitmask;
 }
 
-// One traversal step (Ylitie, Karras, Laine 2017, with triangle postponing). A step either
-// visits the highest-priority internal child of the current node group, or takes up a
-// triangle group popped from the stack. Triangle tests are postponed (the group pushed on
-// the stack) while fewer than `postpone_pct` percent of the warp's active lanes have
-// triangles to test, so that tests run together instead of one lane at a time. Returns true
-// when the ray is finished (s.hit / s.tmax / s.hu / s.hv hold the result). stack_overflow is
-// set, and the ray abandoned, if the tree is deeper than the stack.
-// any_hit: stop at the first hit (shadow rays); a run-time flag so one kernel can trace both kinds.
-template <bool STATS, int SH>
-NGI_D bool trav_step(TravState& s, LaneStack<SH> stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
-                     bool& stack_overflow, TraceStats* stats, int postpone_pct, bool any_hit) {
-#if NGI_WHILE_WHILE
-    if (postpone_pct <= 0) {
-        // node phase: every lane without triangles visits nodes until all lanes hold triangles or
-        // have run out of nodes
-        const unsigned act = __activemask();
-#if NGI_TRI_EXIT_PCT > 0
-        uint2 tg = s.tgroup;
-#else
-        uint2 tg = make_uint2(0u, 0u);
-#endif
-        while (true) {
-            const bool want = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
-#if NGI_NODE_EXIT_PCT > 0
-            // leave the node phase once few lanes still search: the others test their
-            // triangles (or take new rays) instead of waiting for the last searching lanes
-            const unsigned wm = __ballot_sync(act, want);
-            if (wm == 0u || __popc(wm) * 100 < __popc(act) * NGI_NODE_EXIT_PCT) break;
-#else
-            if (!__any_sync(act, want)) break;
-#endif
-            if (want) {
-                const uint32_t hits = s.ngroup.y;
-                const int bit = 31 - __clz(hits);
-                s.ngroup.y &= ~(1u << bit);
-                if (s.ngroup.y > 0x00FFFFFFu) {
-                    if (s.sp == kTraversalStack) {
-                        stack_overflow = true;
-                        s.hit = -1;
-                        s.ngroup = make_uint2(0u, 0u);
-                        s.sp = 0;
-                        continue;
-                    }
-                    stack.put(s.sp++, s.ngroup);
+// One traversal step (Ylitie, Karras, Laine 2017), while-while. In the node phase every lane
+// without triangles visits the highest-priority internal child of its node group until few of
+// the warp's lanes still search (kNodeExitPct); in the triangle phase the lanes test their
+// triangle groups together until few still have some (kTriExitPct), the rest keeping their
+// group in the ray state for the next step. Returns true when the ray is finished (s.hit /
+// s.tmax / s.hu / s.hv hold the result). stack_overflow is set, and the ray abandoned, if the
+// tree is deeper than the stack. any_hit: stop at the first hit (shadow rays); a run-time flag
+// so one kernel can trace both kinds. Every lane of the calling warp that holds a ray calls it.
+template <bool STATS>
+NGI_D bool trav_step(TravState& s, uint2* stack, const CwNode* __restrict__ nodes, const float4* __restrict__ tris,
+                     bool& stack_overflow, TraceStats* stats, bool any_hit) {
+    const unsigned act = __activemask();
+    uint2 tg = s.tgroup;
+    while (true) {
+        const bool want = tg.y == 0u && s.ngroup.y > 0x00FFFFFFu;
+        // leave the node phase once few lanes still search: the others test their triangles
+        // (or take new rays) instead of waiting for the last searching lanes
+        const unsigned wm = __ballot_sync(act, want);
+        if (wm == 0u || __popc(wm) * 100 < __popc(act) * kNodeExitPct) break;
+        if (want) {
+            const uint32_t hits = s.ngroup.y;
+            const int bit = 31 - __clz(hits);
+            s.ngroup.y &= ~(1u << bit);
+            if (s.ngroup.y > 0x00FFFFFFu) {
+                if (s.sp == kTraversalStack) {
+                    stack_overflow = true;
+                    s.hit = -1;
+                    s.ngroup = make_uint2(0u, 0u);
+                    s.sp = 0;
+                    continue;
                 }
-                const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
-                const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
-                const uint32_t node = s.ngroup.x + rel;
-                uint32_t child_base, tri_base, imask;
-                const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
-                if (STATS) stats->nodes++;
-                s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-                tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
-                if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack.get(--s.sp);
+                stack[s.sp++] = s.ngroup;
             }
-        }
-#if NGI_TRI_EXIT_PCT > 0
-        // every lane of `act` stays in this loop until the warp leaves it (the ballot needs them
-        // all): an any-hit ray that is done drops its triangles and returns after the loop
-        bool found = false;
-        while (true) {
-            const unsigned tm = __ballot_sync(act, tg.y != 0u);
-            if (tm == 0u || __popc(tm) * 100 < __popc(act) * NGI_TRI_EXIT_PCT) break;
-            if (tg.y == 0u) continue;
-#else
-        while (tg.y != 0u) {
-#endif
-            const int tb = 31 - __clz(tg.y);
-            tg.y &= ~(1u << tb);
-            const uint32_t ti = tg.x + (uint32_t)tb;
-            const float4* tp = tris + 3 * (size_t)ti;
-            const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-            if (STATS) stats->tris++;
-            float t, u, v;
-            if (tri_intersect(s.rp, p0, p1, p2, s.tmin, s.tmax, t, u, v)) {
-                s.tmax = t;
-                s.hu = u;
-                s.hv = v;
-                s.hit = (int)ti;
-#if NGI_TRI_EXIT_PCT > 0
-                if (any_hit) {
-                    found = true;
-                    tg.y = 0u;
-                }
-#else
-                if (any_hit) return true;
-#endif
-            }
-        }
-#if NGI_TRI_EXIT_PCT > 0
-        s.tgroup = tg;
-        if (found) return true;
-        if (tg.y != 0u) return false;  // the rest of the group in the next step
-#endif
-        if (s.ngroup.y <= 0x00FFFFFFu) {
-            if (s.sp == 0) return true;
-            s.ngroup = stack.get(--s.sp);
-        }
-        return false;
-    }
-#endif
-    uint2 tgroup;
-    if (s.ngroup.y > 0x00FFFFFFu) {
-        const uint32_t hits = s.ngroup.y;
-        const int bit = 31 - __clz(hits);
-        s.ngroup.y &= ~(1u << bit);
-        if (s.ngroup.y > 0x00FFFFFFu) {
-            if (s.sp == kTraversalStack) {
-                stack_overflow = true;
-                s.hit = -1;
-                return true;
-            }
-            stack.put(s.sp++, s.ngroup);
-        }
-        const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
-        const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
-        const uint32_t node = s.ngroup.x + rel;
-        uint32_t child_base, tri_base, imask;
-        const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
-        if (STATS) stats->nodes++;
-        s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
-        tgroup = make_uint2(tri_base, hm & 0x00FFFFFFu);
-    } else {
-        tgroup = s.ngroup;  // a postponed triangle group taken off the stack
-        s.ngroup = make_uint2(0u, 0u);
-    }
-    if (postpone_pct > 0) {
-        const unsigned act = __activemask();
-        const bool has_tri = tgroup.y != 0u;
-        const unsigned tri_lanes = __ballot_sync(act, has_tri);
-        const bool more = s.ngroup.y > 0x00FFFFFFu || s.sp > 0;
-        if (has_tri && more && s.sp < kTraversalStack - 1 && __popc(tri_lanes) * 100 < __popc(act) * postpone_pct) {
-            stack.put(s.sp++, tgroup);
-            tgroup.y = 0u;
+            const uint32_t slot = (uint32_t)(bit - 24) ^ s.octinv;
+            const uint32_t rel = __popc(hits & ~(0xFFFFFFFFu << slot));
+            const uint32_t node = s.ngroup.x + rel;
+            uint32_t child_base, tri_base, imask;
+            const uint32_t hm = intersect_children(nodes, node, s, child_base, tri_base, imask);
+            if (STATS) stats->nodes++;
+            s.ngroup = make_uint2(child_base, (hm & 0xFF000000u) | imask);
+            tg = make_uint2(tri_base, hm & 0x00FFFFFFu);
+            if (s.ngroup.y <= 0x00FFFFFFu && tg.y == 0u && s.sp > 0) s.ngroup = stack[--s.sp];
         }
     }
-    while (tgroup.y != 0u) {
-        const int tb = 31 - __clz(tgroup.y);
-        tgroup.y &= ~(1u << tb);
-        const uint32_t ti = tgroup.x + (uint32_t)tb;
+    // every lane of `act` stays in this loop until the warp leaves it (the ballot needs them
+    // all): an any-hit ray that is done drops its triangles and returns after the loop
+    bool found = false;
+    while (true) {
+        const unsigned tm = __ballot_sync(act, tg.y != 0u);
+        if (tm == 0u || __popc(tm) * 100 < __popc(act) * kTriExitPct) break;
+        if (tg.y == 0u) continue;
+        const int tb = 31 - __clz(tg.y);
+        tg.y &= ~(1u << tb);
+        const uint32_t ti = tg.x + (uint32_t)tb;
         const float4* tp = tris + 3 * (size_t)ti;
         const float4 p0 = __ldg(tp + 0), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
         if (STATS) stats->tris++;
@@ -464,17 +295,21 @@ NGI_D bool trav_step(TravState& s, LaneStack<SH> stack, const CwNode* __restrict
             s.hu = u;
             s.hv = v;
             s.hit = (int)ti;
-            if (any_hit) return true;
+            if (any_hit) {
+                found = true;
+                tg.y = 0u;
+            }
         }
     }
+    s.tgroup = tg;
+    if (found) return true;
+    if (tg.y != 0u) return false;  // the rest of the group in the next step
     if (s.ngroup.y <= 0x00FFFFFFu) {
         if (s.sp == 0) return true;
-        s.ngroup = stack.get(--s.sp);
+        s.ngroup = stack[--s.sp];
     }
     return false;
 }
-
-constexpr int kPostponePct = 0;  // measured fastest on the terrain workload: never postpone
 
 // Whole traversal of one ray (parity hooks and simple callers). Returns the leaf-order
 // triangle index of the nearest hit in [tmin, tmax) (ANY_HIT: of any hit) or -1; on a hit
@@ -487,8 +322,7 @@ NGI_D int trace_ray(const CwNode* __restrict__ nodes, const float4* __restrict__
     TravState s;
     trav_init(s, ox, oy, oz, dx, dy, dz, tmin, tmax);
     uint2 stack[kTraversalStack];
-    const LaneStack<0> ls{stack, 0u};
-    while (!trav_step<STATS, 0>(s, ls, nodes, tris, stack_overflow, stats, 0, ANY_HIT)) {
+    while (!trav_step<STATS>(s, stack, nodes, tris, stack_overflow, stats, ANY_HIT)) {
     }
     if (s.hit >= 0) {
         tmax = s.tmax;

@@ -47,15 +47,11 @@ template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
 // the next hit's triangle and normals (1551); the prefetched lines likely compete with the BVH for L2.
 // No change (1875-1880 against 1875): loading the hit record together with the slot state, and an
 // emitter cdf search in float pairs instead of FP64 (the FP64 pipe is 23% busy in this kernel).
-#ifndef NGI_LOGIC_MIN_BLOCKS
-#define NGI_LOGIC_MIN_BLOCKS 4
-#endif
+constexpr int kLogicMinBlocks = 4;
 // Minimum resident blocks per SM asked of the traversal kernels (register budget). 8 blocks of
 // 128 give 64 registers and no spills. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
 // each): 8: 1809, 6 (80 registers): 1723, 10 (51, 132 B of spills): 1739, 12 (42): 1617.
-#ifndef NGI_TRACE_MIN_BLOCKS
-#define NGI_TRACE_MIN_BLOCKS 8
-#endif
+constexpr int kTraceMinBlocks = 8;
 
 enum : uint8_t { SLOT_EMPTY = 0, SLOT_ACTIVE = 1, SLOT_DONE = 2 };
 
@@ -92,7 +88,6 @@ struct RenderConsts {
     int stratified;
     long long strat_end;    // global sample indices below this are pixel-stratified
     int trace_refill;       // idle lanes that trigger a traversal warp's refill
-    int trace_postpone;     // triangle-postponing threshold (percent of active lanes), -1 = default
     int num_prims;          // primitives of the scene (adjoint gradient layout)
     int ray_offset;         // NGI_RAY_OFFSET_*: absolute tmin = EpsF, or scale-aware origin offsets
     int trace_all;          // NGI_RENDER_TRACE_ALL_RAYS: trace the rays toward hits that cannot score
@@ -501,79 +496,31 @@ NGI_D bool next_hit_is_dead(const RenderConsts& rc, float next_rr, int nv) {
     return next_rr > 0.5f || (rc.max_vertices != -1 && nv + 1 >= rc.max_vertices);
 }
 
-// PART: kLogicFused does both halves of an iteration in one kernel; kLogicShade consumes the
+// PART: kLogicFused does both halves of an iteration in one kernel; kLogicShadeQ consumes the
 // hits, does next-event estimation and continues the paths, handing the slots whose path ended to
 // kLogicRegen, which starts new samples in them (two kernels of half the code each: the fused
 // kernel stalls on instruction fetch). ptdirect runs split (terrain 2091 vs 2059 Mrays/s fused);
 // pt, with no next-event estimation to separate, stays fused (Cornell box 4038 vs 3640 split).
-constexpr int kLogicFused = 0, kLogicShade = 1, kLogicRegen = 2, kLogicShadeQ = 3;
-#ifndef NGI_REGEN_ATTEMPTS
-#define NGI_REGEN_ATTEMPTS 2
-#endif
-constexpr int kRegenAttempts = NGI_REGEN_ATTEMPTS;  // samples a slot may claim per iteration
+// The shading half reads its slots from queues (the slots whose extension ray hit something, and
+// the slots regeneration left empty) instead of scanning every slot of the wave: terrain 1950
+// against 1830 Msamples/s, the 10M-triangle interior 334 against 308.
+constexpr int kLogicFused = 0, kLogicRegen = 2, kLogicShadeQ = 3;
+constexpr int kRegenAttempts = 2;  // samples a slot may claim per iteration
 // Shadow-queue entries per path slot and iteration: one next-event estimation at the slot's
 // vertex plus one sensor connection per sample claimed (bdpt: two connections).
 constexpr size_t kShadowPerSlot = 1 + (kRegenAttempts > 1 ? kRegenAttempts : 1);
-#ifndef NGI_SPLIT_LOGIC
-#define NGI_SPLIT_LOGIC 1
-#endif
-#ifndef NGI_SHADE_MIN_BLOCKS
-#define NGI_SHADE_MIN_BLOCKS 4
-#endif
-#ifndef NGI_REGEN_MIN_BLOCKS
-#define NGI_REGEN_MIN_BLOCKS 4
-#endif
-// Shading in class order: the queued-slot shading kernel sorts each block's items by what their
-// shading does (the BSDF of the hit primitive, a miss, a slot left empty) with a counting sort in
-// shared memory, so that the lanes of a warp take the same branches. Measured on the
-// 1.55M-triangle terrain (Mrays/s, two runs each): 1798-1802 sorted against 1803-1804, the
-// logic's share of GPU time unchanged at 36%: the shading warps do not diverge on the material
-// type. Off by default.
-#ifndef NGI_SHADE_SORT
-#define NGI_SHADE_SORT 0
-#endif
-constexpr int kShadeClasses = 8;
-
-// Item this thread shades after the block's counting sort (a permutation of the block's items;
-// items past n_items stay past it). Every thread of the block must call it.
-template <typename R>
-NGI_D int shade_sort_item(const SceneView<R>& sv, const WaveView<R>& w, int item, int n_items, int n_ext_in) {
-    __shared__ int sort_base[kShadeClasses];
-    __shared__ int sort_item[kLogicBlock];
-    int cls = kShadeClasses - 1;  // empty slot or past the end
-    if (item < n_items && item < n_ext_in) {
-        const int ti = __float_as_int(w.hit[w.ext_in[item]].w);
-        if (ti < 0) {
-            cls = kShadeClasses - 2;
-        } else {
-            const DevMaterial<R>& m = sv.mats[__float_as_int(sv.nrm[3 * (size_t)ti].w)];
-            cls = m.bsdf == BSDF_D ? 0 : m.bsdf == BSDF_G ? 1 : m.bsdf == BSDF_S ? 2 + min(max(m.s_type, 0), 2) : 5;
-        }
-    }
-    if (threadIdx.x < kShadeClasses) sort_base[threadIdx.x] = 0;
-    __syncthreads();
-    const int rank = atomicAdd(&sort_base[cls], 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int c = 0; c < kShadeClasses; c++) {
-            const int n = sort_base[c];
-            sort_base[c] = acc;
-            acc += n;
-        }
-    }
-    __syncthreads();
-    sort_item[sort_base[cls] + rank] = item;
-    __syncthreads();
-    const int sorted = sort_item[threadIdx.x];
-    __syncthreads();  // the arrays are reused by the block's next round of items
-    return sorted;
-}
+// Resident blocks per SM the two ptdirect halves are compiled for (64 registers each). 5 or 6
+// blocks (48 / 40 registers) were slower on the terrain: 2066-2083 against 2103 Mrays/s.
+constexpr int kShadeMinBlocks = 4, kRegenMinBlocks = 4;
+// Measured and not kept: sorting each block's 256 items by class (BSDF of the hit primitive,
+// miss, empty slot) in shared memory before shading: 1798-1802 against 1803-1804 Mrays/s on the
+// terrain, the logic's share of GPU time unchanged at 36%. The shading warps do not diverge on
+// the material type.
 
 template <typename R, bool DIRECT, bool ADJ, bool BATCH = false, int PART = kLogicFused>
-__global__ void __launch_bounds__(256, PART == kLogicFused                          ? NGI_LOGIC_MIN_BLOCKS
-                                       : (PART == kLogicShade || PART == kLogicShadeQ) ? NGI_SHADE_MIN_BLOCKS
-                                                                                     : NGI_REGEN_MIN_BLOCKS) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
+__global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
+                                       : PART == kLogicShadeQ ? kShadeMinBlocks
+                                                              : kRegenMinBlocks) k_logic(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0,
                                                const JobView<R>* __restrict__ jobs, int num_jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && !DIRECT && rc0.num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
@@ -591,10 +538,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused                      
                         : PART == kLogicShadeQ ? n_ext_in + min(*w.carry_in_count, w.Q - n_ext_in)
                                                : w.Q;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += stride) {
-        int item = base + (int)threadIdx.x;
-#if NGI_SHADE_SORT
-        if constexpr (PART == kLogicShadeQ) item = shade_sort_item(sv0, w, item, n_items, n_ext_in);
-#endif
+        const int item = base + (int)threadIdx.x;
         const bool valid = item < n_items;  // false only past the end of a queue
         int s = item;
         uint8_t st;
@@ -719,7 +663,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused                      
             }
         }
 
-        if (PART == kLogicShade || PART == kLogicShadeQ) {
+        if (PART == kLogicShadeQ) {
             // ---- hand the slots whose path ended to the regeneration kernel ----
             const int q = warp_append(&w.ctr->regen_count, need_new);
             if (need_new) w.regen_queue[q] = s;
@@ -1355,28 +1299,22 @@ constexpr int kLogicCamera = 0, kLogicLight = 1, kLogicBdpt = 2;
 // the warp fetches that many new rays with one atomic and the lanes start them while the
 // others carry on. This keeps SIMD lanes busy on incoherent rays (Aila and Laine, HPG 2009)
 // and removes the tail of a fixed grid.
-// KIND 0 traces the extension queue (closest hit), 1 the shadow queue (any hit), 2 both in one
-// launch: extension items first, then shadow items, each lane tracing its own kind, so shadow rays
-// fill the tail of the extension work instead of a second launch.
-template <typename R, int KIND, bool STATS, bool ADJ = false, bool BATCH = false>
-__global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R> sv, WaveView<R> w, int refill, int postpone,
-                                                      int num_prims, const JobView<R>* __restrict__ jobs) {
+// One launch traces both queues: extension items first, then shadow items, each lane tracing its
+// own kind, so shadow rays fill the tail of the extension work instead of a second launch
+// (terrain 1483 against 1417 Mrays/s for two launches).
+template <typename R, bool STATS, bool ADJ = false, bool BATCH = false>
+__global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv, WaveView<R> w, int refill,
+                                                                 int num_prims, const JobView<R>* __restrict__ jobs) {
     extern __shared__ float adj_smem[];
     float* gsm = (ADJ && num_prims <= kAdjSmemPrims) ? adj_smem : nullptr;
     if (ADJ) adj_smem_clear(gsm, num_prims);
-    const int n_ext = KIND == 1 ? 0 : *w.ext_count;
-    const int n = n_ext + (KIND == 0 ? 0 : w.ctr->sh_count);
-    int* fetch = KIND == 1 ? &w.ctr->sh_fetch : &w.ctr->ext_fetch;
+    const int n_ext = *w.ext_count;
+    const int n = n_ext + w.ctr->sh_count;
+    int* fetch = &w.ctr->ext_fetch;
     TravState s;
     uint2 stack[kTraversalStack];
-#if NGI_SMEM_STACK > 0
-    __shared__ uint2 sh_stack[NGI_SMEM_STACK * kStackLanes];
-    const LaneStack<NGI_SMEM_STACK> ls{stack, (uint32_t)__cvta_generic_to_shared(sh_stack + threadIdx.x)};
-#else
-    const LaneStack<0> ls{stack, 0u};
-#endif
     int item = -1, slot = -1, job = 0;
-    bool shadow = KIND == 1;
+    bool shadow = false;
     const CwNode* nodes = sv.nodes;
     const float4* tris = sv.tris;
     int num_nodes = sv.num_nodes;
@@ -1425,8 +1363,7 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
         if (busy == 0u) break;  // no lane has a ray: the refill above found the queue empty
         if (item >= 0) {
             const bool done = num_nodes == 0 ||
-                              trav_step<STATS, NGI_SMEM_STACK>(s, ls, nodes, tris, overflow, shadow ? &ts_sh : &ts, postpone,
-                                                              shadow);
+                              trav_step<STATS>(s, stack, nodes, tris, overflow, shadow ? &ts_sh : &ts, shadow);
             if (done) {
                 if (shadow) {
                     if (s.hit < 0) {
@@ -1463,18 +1400,14 @@ __global__ void __launch_bounds__(128, NGI_TRACE_MIN_BLOCKS) k_trace(SceneView<R
     if (ADJ) adj_flush(w, gsm, num_prims);
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
     if (STATS) {
-        if (KIND != 1) {
-            warp_sum_add(&w.ctr->ext_nodes, ts.nodes);
-            warp_sum_add(&w.ctr->ext_tris, ts.tris);
-        }
-        if (KIND != 0) {
-            warp_sum_add(&w.ctr->sh_nodes, ts_sh.nodes);
-            warp_sum_add(&w.ctr->sh_tris, ts_sh.tris);
-        }
+        warp_sum_add(&w.ctr->ext_nodes, ts.nodes);
+        warp_sum_add(&w.ctr->ext_tris, ts.tris);
+        warp_sum_add(&w.ctr->sh_nodes, ts_sh.nodes);
+        warp_sum_add(&w.ctr->sh_tris, ts_sh.tris);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (KIND != 1) atomicAdd(&w.ctr->stat_ext, (unsigned long long)n_ext);
-        if (KIND != 0) atomicAdd(&w.ctr->stat_shadow, (unsigned long long)(n - n_ext));
+        atomicAdd(&w.ctr->stat_ext, (unsigned long long)n_ext);
+        atomicAdd(&w.ctr->stat_shadow, (unsigned long long)(n - n_ext));
     }
 }
 
@@ -1720,6 +1653,19 @@ void DeviceFree(HostScene& hs) {
     hs.dev = nullptr;
 }
 
+// The scene's buffers, stream and wave live on the device that was current when it was uploaded.
+// Calls that take the caller's device pointers or stream, or that launch on the current device,
+// must be made with that device current: mixing two devices' pointers in one launch fails or
+// faults.
+void RequireSceneDevice(const DeviceScene& ds) {
+    int cur = -1;
+    CUDA_CHECK(cudaGetDevice(&cur));
+    if (cur != ds.device)
+        throw DeviceError("the scene lives on device " + std::to_string(ds.device) + " but device " +
+                              std::to_string(cur) + " is current: make the scene's device current first",
+                          NGI_ERR_INVALID_ARGUMENT);
+}
+
 // ---- render driver ------------------------------------------------------------------------------
 namespace {
 
@@ -1809,25 +1755,11 @@ int grid_for(int items, int block) {
     return std::max(1, std::min(max_blocks, (items + block - 1) / block));
 }
 
-// Preferred shared-memory carve-out (percent of each SM's unified L1 / shared storage) of the
-// traversal and the path-logic kernels; -1 leaves the driver's choice. The driver still gives a
-// kernel the shared memory it needs. Measured on the 1.55M-triangle terrain (Mrays/s, two runs
-// each): driver's choice 1809, traversal at 0 (largest L1) 1768, logic at 0 1810, both 1768.
-#ifndef NGI_TRACE_CARVEOUT
-#define NGI_TRACE_CARVEOUT -1
-#endif
-#ifndef NGI_LOGIC_CARVEOUT
-#define NGI_LOGIC_CARVEOUT -1
-#endif
-template <typename K>
-void set_carveout(K kernel, int pct) {
-    if (pct >= 0) CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
-}
-
-// Blocks of a persistent kernel that fit on the device at once.
+// Blocks of a persistent kernel that fit on the device at once. Measured and not kept: a preferred
+// shared-memory carve-out of 0 (the largest L1) for the traversal (1768 against 1809 Mrays/s on
+// the terrain with the driver's choice) or for the path logic (1810: no change).
 template <typename K>
 int persistent_grid(K kernel, int block) {
-    set_carveout(kernel, NGI_TRACE_CARVEOUT);
     int dev = 0, sms = 152, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1836,41 +1768,19 @@ int persistent_grid(K kernel, int block) {
 }
 
 constexpr int kTraceBlock = 128;
-static_assert(kTraceBlock == kStackLanes, "one shared-memory stack column per traversal thread");
 constexpr int kRefillLanes = 8;
 
-// Grid sizes of the persistent traversal kernels (queried once, outside any graph capture).
+// Grid size of the persistent traversal kernel (queried once per instance, outside any graph capture).
 template <typename R, bool STATS, bool ADJ = false, bool BATCH = false>
-struct TraceGrids {
-    static int ext() {
-        static const int g = persistent_grid(k_trace<R, false, STATS, false, BATCH>, kTraceBlock);
-        return g;
-    }
-    static int shadow() {
-        static const int g = persistent_grid(k_trace<R, true, STATS, ADJ, BATCH>, kTraceBlock);
-        return g;
-    }
-    static int merged() {
-        static const int g = persistent_grid(k_trace<R, 2, STATS, ADJ, BATCH>, kTraceBlock);
-        return g;
-    }
-};
+int trace_grid() {
+    static const int g = persistent_grid(k_trace<R, STATS, ADJ, BATCH>, kTraceBlock);
+    return g;
+}
 
-// One traversal launch per iteration over both queues (KIND 2) instead of two: shadow rays fill
-// the extension launch's tail. Terrain: 1483 vs 1417 Mrays/s.
-#ifndef NGI_MERGED_TRACE
-#define NGI_MERGED_TRACE 1
-#endif
-
-// Compacted shading (ptdirect): the shading kernel visits only the slots with a ray in flight and
-// the slots regeneration left empty, from queues, instead of every slot of the wave. Terrain:
-// 1950 against 1830 Msamples/s; the 10M-triangle interior 334 against 308.
-#ifndef NGI_COMPACT_SHADE
-#define NGI_COMPACT_SHADE 1
-#endif
+// Compacted shading applies to ptdirect's camera paths outside batches.
 template <bool DIRECT, bool BATCH, int LOGIC>
 constexpr bool compact_shading() {
-    return NGI_COMPACT_SHADE && NGI_SPLIT_LOGIC && DIRECT && !BATCH && LOGIC == kLogicCamera;
+    return DIRECT && !BATCH && LOGIC == kLogicCamera;
 }
 
 // Per-iteration counter reset of compacted shading: the queues the iteration fills start empty,
@@ -1899,8 +1809,6 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
                        int g_logic, int g_trace, cudaStream_t stream, cudaEvent_t* ev,
                        const JobView<R>* jobs = nullptr, int num_jobs = 0, int parity = 0) {
     (void)g_trace;
-    const int g_ext = TraceGrids<R, STATS, ADJ, BATCH>::ext();
-    const int g_sh = TraceGrids<R, STATS, ADJ, BATCH>::shadow();
     constexpr bool compact = compact_shading<DIRECT, BATCH, LOGIC>();
     WaveView<R> vq = v;
     if constexpr (compact) {
@@ -1931,54 +1839,14 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     else if constexpr (compact) {
         k_logic<R, DIRECT, ADJ, BATCH, kLogicShadeQ><<<g_logic, kLogicBlock, 0, stream>>>(sv, vq, rc, jobs, num_jobs);
         k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen><<<g_logic, kLogicBlock, 0, stream>>>(sv, vq, rc, jobs, num_jobs);
-    } else if constexpr (NGI_SPLIT_LOGIC && DIRECT && !BATCH) {
-        k_logic<R, DIRECT, ADJ, BATCH, kLogicShade><<<g_logic, kLogicBlock, DIRECT ? 0 : adj_bytes, stream>>>(
-            sv, v, rc, jobs, num_jobs);
-        k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen><<<g_logic, kLogicBlock, DIRECT ? 0 : adj_bytes, stream>>>(
-            sv, v, rc, jobs, num_jobs);
     } else {
         k_logic<R, DIRECT, ADJ, BATCH><<<g_logic, kLogicBlock, DIRECT ? 0 : adj_bytes, stream>>>(sv, v, rc, jobs, num_jobs);
     }
     if (ev) cudaEventRecord(ev[1], stream);
     const int refill = rc.trace_refill > 0 ? rc.trace_refill : kRefillLanes;
-    const int postpone = rc.trace_postpone >= 0 ? rc.trace_postpone : kPostponePct;
-#if NGI_MERGED_TRACE
-    (void)g_ext;
-    (void)g_sh;
-    k_trace<R, 2, STATS, ADJ, BATCH><<<TraceGrids<R, STATS, ADJ, BATCH>::merged(), kTraceBlock, adj_bytes, stream>>>(
-        sv, vq, refill, postpone, rc.num_prims, jobs);
-    if (ev) {
-        cudaEventRecord(ev[2], stream);
-        cudaEventRecord(ev[3], stream);  // no separate shadow launch: its time is inside ev[1]..ev[2]
-    }
-#else
-    k_trace<R, false, STATS, false, BATCH><<<g_ext, kTraceBlock, 0, stream>>>(sv, vq, refill, postpone, rc.num_prims,
-                                                                             jobs);
+    k_trace<R, STATS, ADJ, BATCH><<<trace_grid<R, STATS, ADJ, BATCH>(), kTraceBlock, adj_bytes, stream>>>(
+        sv, vq, refill, rc.num_prims, jobs);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_trace<R, true, STATS, ADJ, BATCH><<<g_sh, kTraceBlock, adj_bytes, stream>>>(sv, vq, refill, postpone,
-                                                                                 rc.num_prims, jobs);
-    if (ev) cudaEventRecord(ev[3], stream);
-#endif
-}
-
-// Carve-out of the camera path-logic kernels a wave launches (once, before any graph capture).
-template <typename R, bool DIRECT, bool ADJ, bool BATCH, int LOGIC>
-void logic_carveout() {
-    if constexpr (NGI_LOGIC_CARVEOUT >= 0 && LOGIC == kLogicCamera) {
-        static const bool once = [] {
-            if constexpr (compact_shading<DIRECT, BATCH, LOGIC>()) {
-                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicShadeQ>, NGI_LOGIC_CARVEOUT);
-                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen>, NGI_LOGIC_CARVEOUT);
-            } else if constexpr (NGI_SPLIT_LOGIC && DIRECT && !BATCH) {
-                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicShade>, NGI_LOGIC_CARVEOUT);
-                set_carveout(k_logic<R, DIRECT, ADJ, BATCH, kLogicRegen>, NGI_LOGIC_CARVEOUT);
-            } else {
-                set_carveout(k_logic<R, DIRECT, ADJ, BATCH>, NGI_LOGIC_CARVEOUT);
-            }
-            return true;
-        }();
-        (void)once;
-    }
 }
 
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
@@ -1998,10 +1866,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         iters_per_graph += iters_per_graph & 1;  // queue parity must restart at 0 with every graph launch
     }
 
-    TraceGrids<R, STATS, ADJ, BATCH>::ext();
-    TraceGrids<R, STATS, ADJ, BATCH>::shadow();
-    TraceGrids<R, STATS, ADJ, BATCH>::merged();
-    logic_carveout<R, DIRECT, ADJ, BATCH, LOGIC>();
+    trace_grid<R, STATS, ADJ, BATCH>();
     cudaGraphExec_t exec = nullptr;
     if (!kernel_timing) {
         cudaGraph_t graph = nullptr;
@@ -2018,8 +1883,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         cudaGraphDestroy(graph);
         if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
     }
-    cudaEvent_t kev[4] = {nullptr, nullptr, nullptr, nullptr};
-    double kms[3] = {0, 0, 0};
+    cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
+    double kms[2] = {0, 0};
     long long launches = 0;
 
     long long iterations = 0;
@@ -2039,8 +1904,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
                 enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LOGIC>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
                                                                        kev, jobs, num_jobs, (int)(iterations & 1));
                 CUDA_CHECK(cudaGetLastError());
-                CUDA_CHECK(cudaEventSynchronize(kev[3]));
-                for (int k = 0; k < 3; k++) {
+                CUDA_CHECK(cudaEventSynchronize(kev[2]));
+                for (int k = 0; k < 2; k++) {
                     float t = 0;
                     CUDA_CHECK(cudaEventElapsedTime(&t, kev[k], kev[k + 1]));
                     kms[k] += t;
@@ -2077,16 +1942,10 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     const WaveCounters& c = *wv->h_ctr;
     ds.last_stats.logic_ms = kms[0];
     ds.last_stats.logic_launches = ds.last_stats.extend_launches = launches;
-#if NGI_MERGED_TRACE
     // one traversal launch traces both queues: its time is extend_ms, no shadow launch exists
-    ds.last_stats.extend_ms = kms[1] + kms[2];
+    ds.last_stats.extend_ms = kms[1];
     ds.last_stats.shadow_ms = 0;
     ds.last_stats.shadow_launches = 0;
-#else
-    ds.last_stats.extend_ms = kms[1];
-    ds.last_stats.shadow_ms = kms[2];
-    ds.last_stats.shadow_launches = launches;
-#endif
     ds.last_stats.extend_nodes = (int64_t)c.ext_nodes;
     ds.last_stats.extend_tris = (int64_t)c.ext_tris;
     ds.last_stats.shadow_nodes = (int64_t)c.sh_nodes;
@@ -2119,11 +1978,32 @@ void ensure_bdpt_buffers(RenderWave* wv, WaveView<R>& v) {
     wv->bdpt_precision = wv->precision;
 }
 
+// Kernel constants of a render with parameters p on a scene of num_prims primitives.
+RenderConsts consts_of(const ngi_render_params& p, int num_prims) {
+    RenderConsts rc{};
+    rc.renderer = p.renderer;
+    rc.max_vertices = p.max_num_vertices;
+    rc.num_samples = p.num_samples;
+    rc.sample_offset = p.sample_offset;
+    rc.seed = p.seed;
+    rc.width = p.width;
+    rc.height = p.height;
+    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
+    const long long wh = (long long)p.width * p.height;
+    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
+    rc.trace_refill = p.trace_refill;
+    rc.ray_offset = p.ray_offset;
+    rc.trace_all = (p.flags & NGI_RENDER_TRACE_ALL_RAYS) ? 1 : 0;
+    rc.num_prims = num_prims;
+    return rc;
+}
+
 }  // namespace
 
 void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cudaStream_t user_stream) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
     if (p.renderer != NGI_RENDERER_PT && ds.num_lights == 0)
         throw DeviceError("this renderer needs at least one light (the reference indexes an empty light list)",
@@ -2143,22 +2023,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
     RenderWave* wv = ensure_wave(ds, Q, p.precision);
-    RenderConsts rc{};
-    rc.renderer = p.renderer;
-    rc.max_vertices = p.max_num_vertices;
-    rc.num_samples = p.num_samples;
-    rc.sample_offset = p.sample_offset;
-    rc.seed = p.seed;
-    rc.width = p.width;
-    rc.height = p.height;
-    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
-    const long long wh = (long long)p.width * p.height;
-    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
-    rc.trace_refill = p.trace_refill;
-    rc.ray_offset = p.ray_offset;
-    rc.trace_all = (p.flags & NGI_RENDER_TRACE_ALL_RAYS) ? 1 : 0;
-    rc.num_prims = (int)hs.prims.size();
-    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
+    const RenderConsts rc = consts_of(p, (int)hs.prims.size());
     const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
@@ -2214,6 +2079,7 @@ __global__ void k_scale(double* film, size_t n, double s) {
 void DeviceRenderToHost(HostScene& hs, const ngi_render_params& p, double* h_film) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     const size_t elems = 3 * (size_t)p.width * (size_t)p.height;
     if (ds.film_elems < elems) {
         if (ds.film) cudaFree(ds.film);
@@ -2237,6 +2103,7 @@ void DeviceRenderToHost(HostScene& hs, const ngi_render_params& p, double* h_fil
 void DeviceIntersect(HostScene& hs, const float* h_rays, int64_t n, int32_t* prim, float* t, float* uv) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     if (n == 0) return;
     float4* d_rays = nullptr;
     int32_t* d_prim = nullptr;
@@ -2275,6 +2142,7 @@ void DeviceIntersect(HostScene& hs, const float* h_rays, int64_t n, int32_t* pri
 void DeviceVisible(HostScene& hs, const double* h_pts, int64_t n, uint8_t* vis) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     if (n == 0) return;
     double* d_pts = nullptr;
     uint8_t* d_vis = nullptr;
@@ -2354,6 +2222,7 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
                           double* grad_emission) {
     DeviceUpload(hs);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
     if (p.renderer == NGI_RENDERER_PTDIRECT && ds.num_lights == 0)
         throw DeviceError("ptdirect needs at least one light", NGI_ERR_UNSUPPORTED);
@@ -2392,22 +2261,7 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
         if ((long long)Q > need) Q = (int)need;
         Q = (Q + 255) / 256 * 256;
         RenderWave* wv = ensure_wave(ds, Q, p.precision);
-        RenderConsts rc{};
-        rc.renderer = p.renderer;
-        rc.max_vertices = p.max_num_vertices;
-        rc.num_samples = p.num_samples;
-        rc.sample_offset = p.sample_offset;
-        rc.seed = p.seed;
-        rc.width = p.width;
-        rc.height = p.height;
-        rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
-        const long long wh = (long long)p.width * p.height;
-        rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
-        rc.trace_refill = p.trace_refill;
-    rc.ray_offset = p.ray_offset;
-    rc.trace_all = (p.flags & NGI_RENDER_TRACE_ALL_RAYS) ? 1 : 0;
-    rc.num_prims = (int)hs.prims.size();
-    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
+        const RenderConsts rc = consts_of(p, (int)hs.prims.size());
         const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
         const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
         if (p.precision == NGI_PRECISION_FP64) {
@@ -2450,26 +2304,6 @@ void ensure_batch_buffers(RenderWave* wv, WaveView<R>& v) {
         v.job = (int*)a;
         v.sh_job = (int*)b;
     }
-}
-
-RenderConsts consts_of(const ngi_render_params& p, int num_prims) {
-    RenderConsts rc{};
-    rc.renderer = p.renderer;
-    rc.max_vertices = p.max_num_vertices;
-    rc.num_samples = p.num_samples;
-    rc.sample_offset = p.sample_offset;
-    rc.seed = p.seed;
-    rc.width = p.width;
-    rc.height = p.height;
-    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
-    const long long wh = (long long)p.width * p.height;
-    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
-    rc.trace_refill = p.trace_refill;
-    rc.ray_offset = p.ray_offset;
-    rc.trace_all = (p.flags & NGI_RENDER_TRACE_ALL_RAYS) ? 1 : 0;
-    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
-    rc.num_prims = num_prims;
-    return rc;
 }
 
 struct BatchConfig {
@@ -2515,7 +2349,6 @@ double batch_pass(std::vector<HostScene*>& scenes, const std::vector<ngi_render_
         rc0.num_samples = total;
         rc0.max_vertices = unbounded ? -1 : max_vertices;
         rc0.trace_refill = cfg.refill;
-        rc0.trace_postpone = -1;
         WaveView<R> vv = v;
         vv.film = d_films;
         if (total > 0) run_wave<R, false, false, false, true>(hs0, wv, vv, rc0, cfg.ipg, false, stream, d_jobs, n);
@@ -2652,6 +2485,7 @@ void DeviceRenderBatch(std::vector<HostScene*>& scenes, const std::vector<ngi_re
         if (scenes[j]->dev->device != scenes[0]->dev->device)
             throw DeviceError("every scene of a batch must live on the same device", NGI_ERR_INVALID_ARGUMENT);
     }
+    RequireSceneDevice(*scenes[0]->dev);
     if (params[0].precision == NGI_PRECISION_FP64) render_batch<double>(scenes, params, films, opt, stats);
     else render_batch<float>(scenes, params, films, opt, stats);
 }
@@ -2663,11 +2497,14 @@ void DeviceRenderBatch(std::vector<HostScene*>& scenes, const std::vector<ngi_re
 // device-memory budget. For them the render's scratch (the wave of path slots, its queues
 // and counters) lives in one file-scope device array instead of per-call allocations.
 //
-// kNoAllocScratchBytes is the fixed size of that array; every GPU that loads this library
-// holds it until the process exits. It bounds the wave at kNoAllocMaxWave path slots (the
-// number of samples per call is not bounded: samples stream through the wave). All calls
-// share the array and it keeps the last call's contents, so each call clears its counters
-// and slot states first; two calls that overlap on the GPU (e.g. on two streams) race on it.
+// kNoAllocScratchBytes is the fixed size of that array. CUDA loads this file's device code on a
+// device lazily, the first time any of it runs there, and reserves the array at that moment; the
+// device keeps it until the process exits. It bounds the wave at kNoAllocMaxWave path slots (the
+// number of samples per call is not bounded: samples stream through the wave). All calls share
+// the array and it keeps the last call's contents, so each call clears its counters and slot
+// states first; two calls that overlap on the GPU (e.g. on two streams) race on it. Each call
+// runs a host loop that reads the wave's counters back and synchronises the stream, so it cannot
+// be made while that stream is being captured into a graph.
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
 constexpr int kNoAllocMaxWave = 1 << 16;
 
@@ -2735,7 +2572,7 @@ unsigned char* noalloc_scratch_address() {
 }
 
 template <typename R, bool DIRECT>
-void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, cudaStream_t stream) {
+void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, int ipg, cudaStream_t stream) {
     DeviceScene& ds = *hs.dev;
     const SceneView<R> sv = make_view<R>(ds);
     const int g_logic = grid_for(v.Q, kLogicBlock);
@@ -2749,9 +2586,9 @@ void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, cuda
     WaveCounters h{};
     long long iterations = 0;
     while (true) {
-        for (int k = 0; k < 4; k++)  // an even count: queue parity restarts at 0
+        for (int k = 0; k < ipg; k++)
             enqueue_iteration<R, DIRECT, false>(sv, v, rc, v.ctr, g_logic, g_trace, stream, nullptr, nullptr, 0, k & 1);
-        iterations += 4;
+        iterations += ipg;
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(&h, v.ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, stream));
         CUDA_CHECK(cudaStreamSynchronize(stream));
@@ -2775,6 +2612,7 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
         throw DeviceError("the scene is not on the device: call ngi_scene_build first (this entry point allocates "
                           "nothing, so it cannot upload the scene)", NGI_ERR_INVALID_ARGUMENT);
     DeviceScene& ds = *hs.dev;
+    RequireSceneDevice(ds);
     if (hs.sensor_prim < 0) throw DeviceError("the scene has no sensor (E) primitive", NGI_ERR_INVALID_ARGUMENT);
     if (p.renderer != NGI_RENDERER_PT && ds.num_lights == 0)
         throw DeviceError("this renderer needs at least one light (the reference indexes an empty light list)",
@@ -2788,28 +2626,19 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
                           NGI_ERR_INVALID_ARGUMENT);
     cudaStream_t stream = user_stream ? user_stream : ds.stream;
     ds.last_stats = ngi_render_stats{};
+    // first call on this device: the array's address (and its reservation, when the render code
+    // was not loaded on the device yet); a call with no samples does only this
+    unsigned char* base = noalloc_scratch_address();
     if (p.num_samples == 0) return;
     int Q = p.wave_size > 0 ? p.wave_size : kNoAllocMaxWave;
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
-    unsigned char* base = noalloc_scratch_address();
-    RenderConsts rc{};
-    rc.renderer = p.renderer;
-    rc.max_vertices = p.max_num_vertices;
-    rc.num_samples = p.num_samples;
-    rc.sample_offset = p.sample_offset;
-    rc.seed = p.seed;
-    rc.width = p.width;
-    rc.height = p.height;
-    rc.stratified = p.raster_mode == NGI_RASTER_STRATIFIED ? 1 : 0;
-    const long long wh = (long long)p.width * p.height;
-    rc.strat_end = ((p.sample_offset + p.num_samples) / wh) * wh;
-    rc.trace_refill = p.trace_refill;
-    rc.ray_offset = p.ray_offset;
-    rc.trace_all = (p.flags & NGI_RENDER_TRACE_ALL_RAYS) ? 1 : 0;
-    rc.num_prims = (int)hs.prims.size();
-    rc.trace_postpone = p.trace_postpone > 0 ? p.trace_postpone - 1 : -1;
+    const RenderConsts rc = consts_of(p, (int)hs.prims.size());
+    // iterations between host checks of the wave's counters; an even count, so that the queue
+    // parity of compacted shading restarts at 0 with every group
+    int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
+    ipg += ipg & 1;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
     if (p.precision == NGI_PRECISION_FP64) {
         WaveView<double> v{};
@@ -2817,16 +2646,16 @@ void DeviceRenderNoAlloc(HostScene& hs, const ngi_render_params& p, double* d_fi
             throw DeviceError("allocation-free scratch too small for the wave", NGI_ERR_INVALID_ARGUMENT);
         carve_wave<double>(base, Q, v);
         v.film = d_film;
-        if (direct) run_wave_noalloc<double, true>(hs, v, rc, stream);
-        else run_wave_noalloc<double, false>(hs, v, rc, stream);
+        if (direct) run_wave_noalloc<double, true>(hs, v, rc, ipg, stream);
+        else run_wave_noalloc<double, false>(hs, v, rc, ipg, stream);
     } else {
         WaveView<float> v{};
         if (carve_wave<float>(nullptr, Q, v) > kNoAllocScratchBytes)
             throw DeviceError("allocation-free scratch too small for the wave", NGI_ERR_INVALID_ARGUMENT);
         carve_wave<float>(base, Q, v);
         v.film = d_film;
-        if (direct) run_wave_noalloc<float, true>(hs, v, rc, stream);
-        else run_wave_noalloc<float, false>(hs, v, rc, stream);
+        if (direct) run_wave_noalloc<float, true>(hs, v, rc, ipg, stream);
+        else run_wave_noalloc<float, false>(hs, v, rc, ipg, stream);
     }
 }
 

@@ -773,6 +773,30 @@ def batch_jobs(num_jobs: int = 256, seed: int = 1000, pool_size: int = 160, max_
     return pool, jobs
 
 
+def _batch_light(lx, lz) -> Mesh:
+    return quad((lx - 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz + 0.7), (lx - 0.7, 6.0, lz + 0.7),
+                (0, -1, 0))
+
+
+def _batch_floor() -> Mesh:
+    return quad((-6, 0, 6), (6, 0, 6), (6, 0, -6), (-6, 0, -6), (0, 1, 0))
+
+
+def batch_job_desc(pool, job) -> SceneDesc:
+    """The scene of one batch job in memory, primitives in the order write_batch writes them
+    (lights, floor, the job's pool subset, camera)."""
+    s = SceneDesc()
+    for lx, lz, le in job["lights"]:
+        t, p = area_light(le)
+        s.primitives.append(Primitive(t, p, _batch_light(lx, lz), "light"))
+    t, p = diffuse((0.5, 0.5, 0.5))
+    s.primitives.append(Primitive(t, p, _batch_floor(), "floor"))
+    for i in job["pool"]:
+        s.primitives.append(pool[i])
+    s.primitives.append(pinhole(job["eye"], (0.0, 0.5, 0.0), (0, 1, 0), 50.0))
+    return s
+
+
 def write_batch(pool, jobs, directory) -> list:
     """Writes the pool's OBJ files once and one YAML per job; returns the YAML paths."""
     d = Path(directory)
@@ -783,9 +807,8 @@ def write_batch(pool, jobs, directory) -> list:
         if not (d / fn).exists():
             write_obj(d / fn, p.mesh, p.name)
         files.append(fn)
-    floor = quad((-6, 0, 6), (6, 0, 6), (6, 0, -6), (-6, 0, -6), (0, 1, 0))
     if not (d / "floor.obj").exists():
-        write_obj(d / "floor.obj", floor, "floor")
+        write_obj(d / "floor.obj", _batch_floor(), "floor")
     paths = []
     for j, job in enumerate(jobs):
         lines = ["version: 5", "scene:", "  primitives:"]
@@ -800,8 +823,7 @@ def write_batch(pool, jobs, directory) -> list:
 
         for k, (lx, lz, le) in enumerate(job["lights"]):
             fn = f"light_{j:04d}_{k}.obj"
-            write_obj(d / fn, quad((lx - 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz - 0.7), (lx + 0.7, 6.0, lz + 0.7),
-                                   (lx - 0.7, 6.0, lz + 0.7), (0, -1, 0)), "light")
+            write_obj(d / fn, _batch_light(lx, lz), "light")
             t, p = area_light(le)
             add(t, p, fn)
         t, p = diffuse((0.5, 0.5, 0.5))

@@ -1364,6 +1364,26 @@ ora_scene* Build(const ora_prim_desc* prims, int n_prims, const float* tri_pos, 
 
 }  // namespace
 
+// Runs fn(i) for i in [0, n) on every hardware thread, in contiguous chunks. Each query is
+// independent, so the results do not depend on the thread count.
+template <typename F>
+void ParallelQueries(int64_t n, F fn) {
+    const int threads = std::max(1, (int)std::thread::hardware_concurrency());
+    const int64_t chunk = 1024;
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (int64_t b = next.fetch_add(chunk); b < n; b = next.fetch_add(chunk))
+            for (int64_t i = b; i < std::min(n, b + chunk); i++) fn(i);
+    };
+    if (n <= chunk || threads == 1) {
+        work();
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int k = 0; k < threads; k++) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+}
+
 extern "C" {
 
 const char* ora_last_error(void) { return g_err.c_str(); }
@@ -1381,7 +1401,7 @@ ora_scene* ora_scene_create(const ora_prim_desc* prims, int32_t n_prims, const f
 void ora_scene_free(ora_scene* s) { delete s; }
 
 int ora_intersect(ora_scene* s, const float* rays, int64_t n, int32_t use_bvh, int32_t* prim, float* t, float* uv) {
-    for (int64_t i = 0; i < n; i++) {
+    ParallelQueries(n, [&](int64_t i) {
         const float* r = rays + 8 * i;
         const float o[3] = {r[0], r[1], r[2]}, d[3] = {r[4], r[5], r[6]};
         const RayF ray = MakeRay(o, d);
@@ -1390,15 +1410,15 @@ int ora_intersect(ora_scene* s, const float* rays, int64_t n, int32_t use_bvh, i
         t[i] = h.tri >= 0 ? h.t : INFINITY;
         uv[2 * i] = h.tri >= 0 ? h.u : 0.0f;
         uv[2 * i + 1] = h.tri >= 0 ? h.v : 0.0f;
-    }
+    });
     return 0;
 }
 
 int ora_visible(ora_scene* s, const double* pts, int64_t n, int32_t use_bvh, uint8_t* vis) {
-    for (int64_t i = 0; i < n; i++) {
+    ParallelQueries(n, [&](int64_t i) {
         const double* q = pts + 6 * i;
         vis[i] = Visible(*s, use_bvh != 0, dv3(q[0], q[1], q[2]), dv3(q[3], q[4], q[5])) ? 1 : 0;
-    }
+    });
     return 0;
 }
 

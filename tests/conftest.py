@@ -47,3 +47,83 @@ def cornell(tmp_path_factory):
 
 def rel_rmse(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+def welch_z(gpu_films: np.ndarray, oracle_films: np.ndarray):
+    """Per-pixel Welch z-scores of the mean of K independent GPU films against the mean of K
+    independent oracle films (same expectation, different random numbers), over the pixels
+    where either side has variance. Returns (z, ratio of the image sums)."""
+    K1, K2 = len(gpu_films), len(oracle_films)
+    mg, mo = gpu_films.mean(0), oracle_films.mean(0)
+    se = np.sqrt(gpu_films.var(0, ddof=1) / K1 + oracle_films.var(0, ddof=1) / K2)
+    ok = se > 0
+    return (mg[ok] - mo[ok]) / se[ok], float(mg.sum() / max(mo.sum(), 1e-300))
+
+
+def camera_rays(desc, n: int, aspect: float, rng, tmin: float = 1e-4) -> np.ndarray:
+    """n rays (ox, oy, oz, tmin, dx, dy, dz, tmax) from the scene's pinhole eye through uniform
+    raster positions of its vertical field of view: the directions a camera pass traces."""
+    cam = None
+    for p in desc.primitives:
+        if "E" in p.type and p.params["E"]["type"] == "pinhole":
+            cam = p.params["E"]["pinhole"]
+    eye = np.asarray(cam["view"]["eye"], np.float64)
+    fwd = np.asarray(cam["view"]["center"], np.float64) - eye
+    fwd /= np.linalg.norm(fwd)
+    right = np.cross(fwd, np.asarray(cam["view"]["up"], np.float64))
+    right /= np.linalg.norm(right)
+    up = np.cross(right, fwd)
+    th = np.tan(np.radians(cam["perspective"]["fov"]) / 2)
+    r = rng.uniform(0.0, 1.0, (n, 2))
+    d = fwd + ((2 * r[:, :1] - 1) * th * aspect) * right + ((2 * r[:, 1:] - 1) * th) * up
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = eye.astype(np.float32)
+    rays[:, 3] = tmin
+    rays[:, 4:7] = d.astype(np.float32)
+    rays[:, 7] = np.float32(3.4e38)
+    return rays
+
+
+def bounce_rays(rays: np.ndarray, prim: np.ndarray, t: np.ndarray, rng, tmin: float = 1e-4) -> np.ndarray:
+    """Second-bounce rays: from the hit points of `rays` (where prim >= 0) in uniform random
+    directions, as extension rays leave a surface."""
+    hit = prim >= 0
+    o = rays[hit, 0:3].astype(np.float64) + rays[hit, 4:7].astype(np.float64) * t[hit, None].astype(np.float64)
+    d = rng.normal(size=o.shape)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    out = np.zeros((len(o), 8), np.float32)
+    out[:, 0:3] = o.astype(np.float32)
+    out[:, 3] = tmin
+    out[:, 4:7] = d.astype(np.float32)
+    out[:, 7] = np.float32(3.4e38)
+    return out
+
+
+T_REL_TOL = 1e-5  # hit-distance tolerance
+
+
+def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999):
+    """First hits of the GPU traversal against the oracle's for the same rays.
+
+    Hit / miss agree; primitive ids are bit-exact on every ray whose nearest hit is not a tie
+    (two triangles at the identical distance, where traversal order picks one: there the
+    distances must still be identical); hit distances are within T_REL_TOL everywhere and
+    bit-identical on at least `min_exact` of the rays; barycentrics agree to 1e-6.
+    Returns (hit rays compared, ties) for reporting."""
+    gp, gt, guv = gpu
+    op, ot, ouv = ora
+    miss_agree = (gp < 0) == (op < 0)
+    assert miss_agree.mean() > 0.9999, f"{label}: hit/miss disagree on {(~miss_agree).sum()} rays"
+    both = (gp >= 0) & (op >= 0)
+    same = gp[both] == op[both]
+    tie = ~same
+    assert np.array_equal(gt[both][tie], ot[both][tie]), f"{label}: primitive ids differ on non-tie rays"
+    assert tie.mean() <= max_tie_share, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
+    rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
+    assert rel.max() <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
+    exact = (gt[both][same] == ot[both][same]).mean() if same.any() else 1.0
+    assert exact >= min_exact, f"{label}: only {exact:.6f} of hit distances are bit-identical"
+    if same.any():
+        assert np.abs(guv[both][same] - ouv[both][same]).max() <= 1e-6
+    return int(both.sum()), int(tie.sum())

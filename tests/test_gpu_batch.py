@@ -1,7 +1,8 @@
 """Batched renders (ngi_render_batch): many independent jobs through one persistent wave.
 
 Every job of a batch traces the Philox paths it traces when rendered alone with the same
-parameters, whatever the mix of scenes, renderers, resolutions, sample counts and path
+parameters -- and that the oracle traces for it (ProcessSample_PT / _PTDirect,
+src/nanogi.cpp:446-802) -- whatever the mix of scenes, renderers, resolutions, sample counts and path
 lengths, with and without the autotuner:
 * plain FP64 path: the films are equal up to the FP64 summation order (1e-9);
 * tuned FP32 path: the batch and single-job kernels are separate compilations, so FP32
@@ -25,7 +26,7 @@ def batch_scenes(native_lib, tmp_path_factory):
     paths = scenegen.write_batch(pool, jobs, tmp_path_factory.mktemp("batch"))
     scenes = [ng.Scene.load(p, 1.0) for p in paths]
     cornell = ng.Scene.load(scenegen.write_scene(scenegen.cornell_box(), tmp_path_factory.mktemp("cb")), 1.0)
-    yield scenes, jobs, cornell
+    yield scenes, jobs, cornell, pool
     for s in scenes:
         s.close()
     cornell.close()
@@ -34,7 +35,7 @@ def batch_scenes(native_lib, tmp_path_factory):
 def _jobs(batch_scenes, scale=1, precision="fp32"):
     import nanogi_gb300 as ng
 
-    scenes, jobs, cornell = batch_scenes
+    scenes, jobs, cornell, _ = batch_scenes
     out = []
     for k, (s, j) in enumerate(zip(scenes, jobs)):
         res = max(8, j["res"] // 8)
@@ -96,3 +97,33 @@ def test_batch_rejects_mixed_precision_and_bad_jobs(batch_scenes):
     assert "job 1" in str(e.value)
     films, st = ng.render_batch([])
     assert films == [] and st["samples"] == 0
+
+
+def test_batch_jobs_replay_the_oracle(batch_scenes):
+    """Three jobs of one FP64 batch (different scenes, renderers, sizes and path lengths)
+    against the oracle replaying the same Philox paths."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+    from oracle.oracle import OracleScene
+
+    from conftest import rel_rmse
+
+    scenes, jobs, _, pool = batch_scenes
+    picked = []
+    for k in range(3):
+        res = 12 + 4 * k
+        r = ng.Renderer(renderer="pt" if k == 0 else "ptdirect", num_samples=res * res * 6 + k,
+                        max_num_vertices=jobs[k]["max_vertices"], width=res, height=res, seed=jobs[k]["seed"],
+                        precision="fp64")
+        picked.append((scenes[k], r))
+    films, st = ng.render_batch(picked)
+    assert st["samples"] == sum(r.num_samples for _, r in picked)
+    for k, ((_, r), f) in enumerate(zip(picked, films)):
+        ora = OracleScene.from_desc(scenegen.batch_job_desc(pool, jobs[k]), 1.0)
+        ref = ora.render(r.renderer, num_samples=r.num_samples, max_vertices=r.max_num_vertices, width=r.width,
+                         height=r.height, seed=r.seed, rng_mode="replay", use_bvh=True)
+        err = rel_rmse(f, ref)
+        print(f"job {k} ({r.renderer}, {r.width}x{r.height}, M={r.max_num_vertices}): rel-RMSE {err:.3e}")
+        assert float(ref.sum()) > 0
+        assert err < 1e-6
+        ora.close()

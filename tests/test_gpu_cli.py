@@ -1,5 +1,6 @@
 """The nanogi command line on the GPU: renderer names, the time budget and progress images
-(src/nanogi.cpp:356-404, 2000-2023)."""
+(src/nanogi.cpp:356-404, 2000-2023), and that its film is the library's film for the same
+parameters (`-n` is the total number of samples, nanogi.cpp:2006)."""
 from __future__ import annotations
 
 import subprocess
@@ -41,3 +42,24 @@ def test_cli_time_budget_writes_progress_images(native_lib, cornell, tmp_path):
     last = ng.load_hdr(images[-1], 32, 32)
     final = ng.load_hdr(out, 32, 32)
     assert last.mean() > 0 and abs(last.mean() / final.mean() - 1) < 0.2
+
+
+@pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
+def test_cli_film_matches_the_library(native_lib, cornell, tmp_path, renderer):
+    import nanogi_gb300 as ng
+
+    _, path = cornell
+    W, H, N = 16, 12, 16 * 12 * 20 + 7
+    out = tmp_path / "film.pfm"
+    cli = ROOT / "nanogi_gb300" / "_build" / "nanogi"
+    r = subprocess.run([str(cli), renderer, str(path), str(out), str(W), str(H), "-n", str(N), "-m", "6", "--seed",
+                        "3", "--precision", "fp64"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    cli_film = ng.load_texture(out)[::-1].astype(np.float64)  # PFM rows read top first; film row 0 = bottom
+    scene = ng.Scene.load(path, W / H)
+    lib_film = ng.Renderer(renderer=renderer, num_samples=N, max_num_vertices=6, width=W, height=H, seed=3,
+                           precision="fp64").render(scene)
+    scene.close()
+    assert float(lib_film.sum()) > 0
+    # the .pfm holds float32: the same film to float rounding
+    assert np.allclose(cli_film, lib_film.astype(np.float32).astype(np.float64), rtol=1e-6, atol=1e-7)

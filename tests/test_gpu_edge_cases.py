@@ -117,7 +117,7 @@ def test_sample_ranges_add_up(native_lib, cornell):
 
 @pytest.mark.parametrize("knobs", [dict(wave_size=256), dict(wave_size=4096, iterations_per_graph=1),
                                    dict(wave_size=1 << 20, iterations_per_graph=16), dict(trace_refill=1),
-                                   dict(trace_refill=32), dict(trace_postpone=51), dict(trace_postpone=1)])
+                                   dict(trace_refill=32)])
 def test_launch_shape_does_not_change_the_film(native_lib, cornell, knobs):
     desc, path = cornell
     W, H = 16, 16

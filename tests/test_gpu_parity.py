@@ -11,11 +11,9 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import rel_rmse
+from conftest import T_REL_TOL, check_hits, rel_rmse
 
 pytestmark = pytest.mark.gpu
-
-T_REL_TOL = 1e-5  # hit-distance tolerance
 
 
 def _random_rays(n, lo, hi, rng, tmin=1e-4):
@@ -28,25 +26,6 @@ def _random_rays(n, lo, hi, rng, tmin=1e-4):
     rays[:, 4:7] = d.astype(np.float32)
     rays[:, 7] = np.float32(3.4e38)
     return rays
-
-
-def _check_hits(gpu, ora, label):
-    gp, gt, guv = gpu
-    op, ot, ouv = ora
-    miss_agree = (gp < 0) == (op < 0)
-    assert miss_agree.mean() > 0.9999, f"{label}: hit/miss disagree on {(~miss_agree).sum()} rays"
-    both = (gp >= 0) & (op >= 0)
-    same = gp[both] == op[both]
-    # A different primitive is only allowed for a tie: two triangles at the very same
-    # distance (e.g. coplanar faces), where traversal order picks one of them.
-    tie = ~same
-    assert np.array_equal(gt[both][tie], ot[both][tie]), f"{label}: primitive ids differ on non-tie rays"
-    assert tie.mean() < 0.01, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
-    rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
-    assert rel.max() <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
-    exact = (gt[both][same] == ot[both][same]).mean()
-    assert exact > 0.999, f"{label}: only {exact:.4f} of hit distances are bit-identical"
-    assert np.abs(guv[both][same] - ouv[both][same]).max() <= 1e-6
 
 
 def _load(desc, tmp_path, aspect=1.0):
@@ -64,7 +43,7 @@ def test_intersect_cornell_bit_exact(native_lib, cornell, tmp_path):
     scene, ora = _load(scenegen.cornell_box(), tmp_path)
     rng = np.random.default_rng(1)
     rays = _random_rays(200_000, -0.2, 1.2, rng)
-    _check_hits(scene.intersect(rays), ora.intersect(rays, use_bvh=False), "cornell")
+    check_hits(scene.intersect(rays), ora.intersect(rays, use_bvh=False), "cornell")
     info = scene.info()
     assert info["device_ready"] == 1 and info["bvh_nodes"] >= 1
 
@@ -77,9 +56,9 @@ def test_intersect_sphere_field_bit_exact(native_lib, tmp_path):
     rng = np.random.default_rng(2)
     rays = _random_rays(20_000, -8.0, 8.0, rng)
     gpu = scene.intersect(rays)
-    _check_hits(gpu, ora.intersect(rays, use_bvh=False), "sphere_field/brute")
+    check_hits(gpu, ora.intersect(rays, use_bvh=False), "sphere_field/brute")
     rays2 = _random_rays(200_000, -8.0, 8.0, rng)
-    _check_hits(scene.intersect(rays2), ora.intersect(rays2, use_bvh=True), "sphere_field/bvh")
+    check_hits(scene.intersect(rays2), ora.intersect(rays2, use_bvh=True), "sphere_field/bvh")
 
 
 def test_intersect_edge_cases(native_lib, tmp_path):

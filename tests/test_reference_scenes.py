@@ -6,9 +6,10 @@ faces). They carry no expected images, so they pin only the loader: every primit
 triangles, the light and sensor, and the scene bounds are compared with a plain parse of the
 OBJ files (polygons split as fans from their first vertex, as the loader documents).
 
-The files are read where the reference tree lies (NGI_REFERENCE_ROOT, default
-/root/reference); nothing is copied into this repository, and the test is skipped where that
-tree is absent.
+The files are read where the reference tree lies (the NGI_REFERENCE_ROOT environment
+variable); the tests are skipped when it is unset or the tree is absent. The last test checks
+that tests/golden/reference_scenes.npz, the fixture the GPU tests render these scenes from,
+still holds exactly what the loader reads from the reference's files.
 """
 from __future__ import annotations
 
@@ -18,11 +19,20 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-REF = Path(os.environ.get("NGI_REFERENCE_ROOT", "/root/reference"))
-SCENES = {
-    "runc": REF / "utils" / "runc" / "data" / "scene.yml",
-    "cornelbox": REF / "utils" / "runc" / "data" / "cornelbox" / "scene.yml",
+REF = Path(os.environ["NGI_REFERENCE_ROOT"]) if os.environ.get("NGI_REFERENCE_ROOT") else None
+SCENE_FILES = {
+    "runc": Path("utils") / "runc" / "data" / "scene.yml",
+    "cornelbox": Path("utils") / "runc" / "data" / "cornelbox" / "scene.yml",
 }
+
+
+def _scene_file(name: str) -> Path:
+    if REF is None:
+        pytest.skip("NGI_REFERENCE_ROOT is not set")
+    yml = REF / SCENE_FILES[name]
+    if not yml.exists():
+        pytest.skip("the reference's example scenes are not present under NGI_REFERENCE_ROOT")
+    return yml
 
 
 def _obj_triangles(path: Path) -> np.ndarray:
@@ -61,11 +71,9 @@ def _tri_key(t: np.ndarray) -> tuple:
     return tuple(sorted(tuple(float(c) for c in v) for v in t))
 
 
-@pytest.mark.parametrize("name", sorted(SCENES))
+@pytest.mark.parametrize("name", sorted(SCENE_FILES))
 def test_reference_example_scene_loads_unchanged(native_lib, name):
-    yml = SCENES[name]
-    if not yml.exists():
-        pytest.skip("the reference's example scenes are not present on this machine")
+    yml = _scene_file(name)
     import nanogi_gb300 as ng
 
     meshes = _mesh_paths(yml)
@@ -90,3 +98,21 @@ def test_reference_example_scene_loads_unchanged(native_lib, name):
         assert sorted(_tri_key(t) for t in got) == sorted(_tri_key(t) for t in want), (name, mp.name)
     allv = np.concatenate(expect_all).reshape(-1, 3)
     assert np.allclose(info["bound_min"], allv.min(0)) and np.allclose(info["bound_max"], allv.max(0))
+
+
+@pytest.mark.parametrize("name", sorted(SCENE_FILES))
+def test_fixture_matches_the_reference_scene(native_lib, name):
+    """tests/golden/reference_scenes.npz holds the scene the loader reads from the reference."""
+    import json
+    import sys
+
+    yml = _scene_file(name)
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_reference_scenes import scene_arrays
+
+    prims, pos, nrm, prim = scene_arrays(yml)
+    d = np.load(Path(__file__).resolve().parent / "golden" / "reference_scenes.npz")
+    assert json.loads(bytes(d[f"{name}_prims"]).decode()) == prims
+    assert np.array_equal(d[f"{name}_pos"], pos)
+    assert np.array_equal(d[f"{name}_nrm"], nrm)
+    assert np.array_equal(d[f"{name}_prim"], prim)

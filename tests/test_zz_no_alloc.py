@@ -57,31 +57,83 @@ def test_noalloc_matches_regular_entry_point(native_lib, built_scene, renderer, 
     check(lib.ngi_render_device(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(ref.data_ptr()), None))
     torch.cuda.synchronize()
     assert float(ref.abs().sum()) > 0
-    for call in range(2):
-        out = _film(torch)
+    # both output films exist before the measured window: the calls below must not allocate
+    outs = [_film(torch), _film(torch)]
+    for call, out in enumerate(outs):
+        if call == 1:
+            torch.cuda.synchronize()
+            free_before = torch.cuda.mem_get_info()[0]
         check(lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()),
                                             None))
         torch.cuda.synchronize()
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free_before, "the allocation-free call changed free device memory"
         assert torch.allclose(out, ref, rtol=RTOL, atol=ATOL), f"call {call + 1} differs"
         st = built_scene.last_stats()
         assert st["camera_rays"] == W * H * SPP
+
+
+def test_noalloc_zero_samples_only_sets_up(native_lib, built_scene):
+    import torch
+
+    import nanogi_gb300 as ng
+    from nanogi_gb300.capi import check
+
+    lib = native_lib
+    out = _film(torch)
+    p = ng.Renderer(renderer="ptdirect", num_samples=0, max_num_vertices=8, width=W, height=H).params()
+    check(lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert not bool(out.any())
+    assert built_scene.last_stats()["camera_rays"] == 0
 
 
 def test_noalloc_rejects_what_it_cannot_do(native_lib, built_scene, cornell):
     import torch
 
     import nanogi_gb300 as ng
-    from nanogi_gb300.capi import RenderParams
+    from nanogi_gb300.capi import RENDERERS, RenderParams
 
     lib = native_lib
     out = _film(torch)
     p = RenderParams(renderer=1, max_num_vertices=8, num_samples=100, width=W, height=H, wave_size=65536 + 256)
     st = lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()), None)
     assert st == 1 and b"exceeds" in lib.ngi_last_error()
+    p.wave_size = 0
+    # the light tracers and bdpt are refused (NGI_ERR_UNSUPPORTED)
+    for name in ("lt", "ltdirect", "bdpt"):
+        p.renderer = RENDERERS[name]
+        st = lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()),
+                                           None)
+        assert st == 7, name
+    p.renderer = 1
+    # measurement flags need buffers of their own
+    p.flags = 1
+    st = lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()), None)
+    assert st == 1
+    p.flags = 0
+    torch.cuda.synchronize()
+    assert not bool(out.any())
     # a scene that was never uploaded cannot be rendered without allocating
     _, path = cornell
     fresh = ng.Scene.load(path, W / H)
-    p.wave_size = 0
     st = lib.ngi_render_device_noalloc(fresh.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()), None)
     assert st == 1 and b"ngi_scene_build" in lib.ngi_last_error()
     fresh.close()
+
+
+def test_noalloc_refuses_another_current_device(native_lib, built_scene):
+    """A scene built on device 0 is not rendered while another device is current."""
+    import torch
+
+    import nanogi_gb300 as ng
+
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs a second visible GPU")
+    lib = native_lib
+    out = _film(torch)
+    p = ng.Renderer(renderer="ptdirect", num_samples=W * H, max_num_vertices=8, width=W, height=H).params()
+    with torch.cuda.device(1):
+        st = lib.ngi_render_device_noalloc(built_scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()),
+                                           None)
+    assert st == 1 and b"current" in lib.ngi_last_error()
