@@ -17,6 +17,13 @@ Reported (one JSON line on rank 0):
              in, normalised film copied to pinned host memory every step
   roofline   the dominant traversal kernel's algorithmic bytes per launch / its CUDA-event
              duration, against the measured HBM copy bandwidth
+  roofline_logic  the same for the path-logic kernels (shading + regeneration) of an iteration
+  time_to_1pct  the metric's second part: seconds to rel-RMSE 1% against an FP64 reference for
+             the tuned (FP32 shading) and the plain (FP64 shading and path state) GPU path, pt on
+             the 256 x 256 Cornell box at max length 8, from two spp rungs each and the spp^-1/2
+             fit (reference: FP64 at 16,384 spp in two halves, its noise subtracted)
+  adjoint    the metric's third part: path-replay backward time over forward time (ptdirect,
+             512 x 512, 64 spp, 64 diffuse material groups)
   cpu_baseline  the CPU oracle (the reference's algorithm restated, FP64, mt19937 stream)
              on this host's cores over a bounded sample of the same workload
 `--impl reference` times that CPU implementation alone, with all host threads.
@@ -79,6 +86,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample duration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the time-to-1% and adjoint measurements")
     ap.add_argument("--scene-dir", default=None)
     ap.add_argument("--wave-size", type=int, default=0, help="path slots (0 = library default)")
     ap.add_argument("--trace-refill", type=int, default=0, help="traversal refill threshold (0 = default)")
@@ -223,6 +231,110 @@ def cpu_baseline(desc, spp_rays_hint, seconds, threads=0):
             "msamples_per_s": n / st["seconds"] / 1e6}
 
 
+# Algorithmic bytes of the path-logic kernels (FP32 path state), per unit of work:
+# * a shaded slot (ptdirect shading half, one per traced extension ray): reads its queue entry
+#   (4), hit record (16), ray origin and direction (32), throughput (16), pixel (4), sample id
+#   (8), vertex count (4), the hit triangle's vertices (48) and shading normals (48) = 180 B;
+#   writes the next ray (32), throughput (16), vertex count (4), state (1) and a queue entry (4) = 57 B;
+# * a started sample (regeneration half): reads its queue entry (4); writes ray (32),
+#   throughput (16), pixel (4), sample id (8), vertex count (4), state (1), queue entry (4) = 73 B;
+# * a shadow ray appended (next-event estimation, either half): origin, direction,
+#   contribution, pixel = 52 B.
+# Materials, lights and the emitter CDF are a few KB that stay in L1/L2 and are not counted.
+LOGIC_BYTES_SHADED, LOGIC_BYTES_STARTED, LOGIC_BYTES_SHADOW = 180 + 57, 4 + 69, 52
+
+
+def roofline_logic(st_t, st_c, peak):
+    launches = max(st_t["logic_launches"], 1)
+    alg = (LOGIC_BYTES_SHADED * st_c["extension_rays"] + LOGIC_BYTES_STARTED * st_c["camera_rays"]
+           + LOGIC_BYTES_SHADOW * st_c["shadow_rays"])
+    per_launch_ms = st_t["logic_ms"] / launches
+    achieved = alg / launches / (per_launch_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_logic (shading + regeneration, one iteration)",
+            "algorithmic_bytes_per_launch": alg / launches, "avg_launch_ms": per_launch_ms,
+            "bytes_per_unit": {"shaded_slot": LOGIC_BYTES_SHADED, "started_sample": LOGIC_BYTES_STARTED,
+                               "shadow_ray": LOGIC_BYTES_SHADOW}}
+
+
+def _fit_spp_to_1pct(rungs):
+    """Least-squares fit of log(err) = log(c) - a log(spp) over the rungs (a = 1/2 for Monte
+    Carlo noise), and spp at 1% from the fit with a = 1/2 held fixed (c from the rungs)."""
+    x = np.log([r["spp"] for r in rungs])
+    y = np.log([max(r["rel_rmse_corrected"], 1e-12) for r in rungs])
+    slope = float(np.polyfit(x, y, 1)[0]) if len(rungs) > 1 else float("nan")
+    logc = float(np.mean(y + 0.5 * x))  # c with the exponent -1/2
+    return {"fitted_exponent": slope, "c_at_half": float(np.exp(logc)),
+            "spp_to_1pct": float((np.exp(logc) / 0.01) ** 2)}
+
+
+def time_to_1pct(ng, ref_spp=16384, rungs=(256, 1024), w=256, h=256, m=8):
+    """Seconds to rel-RMSE 1% for the tuned (fp32) and plain (fp64) GPU pt on the Cornell box."""
+    from nanogi_gb300 import scenegen
+
+    d = tempfile.mkdtemp(prefix="ngi_cornell_")
+    scene = ng.Scene.load(scenegen.write_scene(scenegen.cornell_box(), d), w / h)
+    scene.build()
+
+    def render(renderer, precision, spp, seed, offset=0):
+        r = ng.Renderer(renderer=renderer, num_samples=w * h * spp, max_num_vertices=m, width=w, height=h,
+                        seed=seed, sample_offset=offset, precision=precision)
+        f = r.render(scene).copy()
+        return f, r.last_stats["render_ms"] / 1e3
+
+    def rel(a, b):
+        return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+    # FP64 reference: ptdirect (same image as pt on this scene: area light, no specular surfaces,
+    # lower variance), two independent halves; their difference gives the reference's own noise
+    half = ref_spp // 2
+    ra, ta = render("ptdirect", "fp64", half, 1001)
+    rb, tb = render("ptdirect", "fp64", half, 1001, offset=w * h * half)
+    ref = 0.5 * (ra + rb)
+    sigma_ref = rel(ra, rb) / 2.0
+    out = {"workload": f"cornell_box 36 tris, {w}x{h}, pt, max length {m}",
+           "reference": {"renderer": "ptdirect", "precision": "fp64", "spp": ref_spp, "seconds": ta + tb,
+                         "rel_noise": sigma_ref}}
+    render("pt", "fp32", 16, 3)  # warm both instances
+    render("pt", "fp64", 16, 3)
+    for precision in ("fp32", "fp64"):
+        rs = []
+        for spp in rungs:
+            film, sec = render("pt", precision, spp, 7)
+            err = rel(film, ref)
+            rs.append({"spp": spp, "seconds": sec, "rel_rmse": err,
+                       "rel_rmse_corrected": float(np.sqrt(max(err * err - sigma_ref * sigma_ref, 0.0)))})
+        fit = _fit_spp_to_1pct(rs)
+        sec_per_spp = rs[-1]["seconds"] / rs[-1]["spp"]
+        out[precision] = {"rungs": rs, "fit": fit, "seconds_per_spp": sec_per_spp,
+                          "seconds": fit["spp_to_1pct"] * sec_per_spp}
+    out["fp64_over_fp32"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+    scene.close()
+    return out
+
+
+def adjoint_cost(ng, w=512, h=512, spp=64, m=8, repeats=5):
+    """Device time of the path-replay backward pass over the forward pass (ngi_render_backward
+    against ngi_render with the same parameters)."""
+    from nanogi_gb300 import scenegen
+
+    d = tempfile.mkdtemp(prefix="ngi_inverse_")
+    scene = ng.Scene.load(scenegen.write_scene(scenegen.inverse_box(seed=5, emitter_seed=7), d), w / h)
+    scene.build()
+    r = ng.Renderer(renderer="ptdirect", num_samples=w * h * spp, max_num_vertices=m, width=w, height=h, seed=3)
+    target = np.zeros((h, w, 3))
+    fwd, bwd = [], []
+    for k in range(repeats + 1):
+        img = r.render(scene)
+        fwd.append(r.last_stats["render_ms"])
+        r.backward(scene, 2.0 * (img - target))
+        bwd.append(r.last_stats["render_ms"])
+    fwd, bwd = float(np.median(fwd[1:])), float(np.median(bwd[1:]))
+    scene.close()
+    return {"workload": f"inverse_box 64 diffuse groups + 2 emitters, {w}x{h}, ptdirect, {spp} spp, max length {m}",
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -239,6 +351,7 @@ def run_reference(args):
         ora.render(RENDERER, num_samples=n_step // 4, max_vertices=MAX_VERTICES, width=WIDTH, height=HEIGHT,
                    seed=100 + i, rng_mode="reference", grain=1000)
     rays = 0
+    samples = 0
     secs = 0.0
     threads = 0
     for i in range(args.steps):
@@ -246,6 +359,7 @@ def run_reference(args):
                    rng_mode="reference", grain=1000, sample_offset=i * n_step)
         st = ora.last_stats
         rays += st["extension_rays"] + st["shadow_rays"]
+        samples += st["camera_rays"]
         secs += st["seconds"]
         threads = st["threads"]
     value = rays / secs / 1e6
@@ -258,6 +372,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} x {n_step} samples of the {WIDTH}x{HEIGHT} frame"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "msamples_per_s": samples / secs / 1e6, "rays_per_sample": rays / max(samples, 1),
     }
     print(json.dumps(line), flush=True)
 
@@ -322,7 +437,9 @@ def main():
             st = render_step(base + (args.warmup + i) * n_step)
             totals["rays"] += st["extension_rays"] + st["shadow_rays"]
             totals["samples"] += st["camera_rays"]
-            totals["launches"] += 3 * st["iterations"]
+            # ptdirect: counter reset, shading, regeneration and traversal per iteration, plus the
+            # wave's initial carry queue; pt: the fused path logic and traversal
+            totals["launches"] += (4 * st["iterations"] + 1) if RENDERER == "ptdirect" else 2 * st["iterations"]
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -362,13 +479,21 @@ def main():
     peak, peak_kind = measured_peak()
     frac_dram = ncu_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": frac_dram * per_launch_bytes if frac_dram else None, "kernel": top,
+                "traffic": frac_dram * per_launch_bytes if frac_dram else None,
+                "traffic_source": ("not measured in this run: the DRAM share of the algorithmic bytes from the "
+                                   "committed ncu capture of this kernel on this workload, times this run's "
+                                   "algorithmic bytes per launch") if frac_dram else None,
+                "binding_limit": "instruction issue (the BVH is L2-resident; DRAM carries a small share of "
+                                 "these bytes)",
+                "kernel": top,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
                 "avg_launch_ms": per_launch_ms,
                 "nodes_per_ray": st_c["extend_nodes"] / max(st_c["extension_rays"], 1),
                 "tris_per_ray": st_c["extend_tris"] / max(st_c["extension_rays"], 1),
                 "traced_rays_per_launch": rays_k / max(launches, 1),
                 "kernel_ms_share": {k: v / max(sum(kern.values()), 1e-9) for k, v in kern.items()}}
+
+    rl_logic = roofline_logic(st_t, st_c, peak)
 
     # ---- end to end through the host-buffer C ABI entry point ----
     host_film = torch.empty((HEIGHT, WIDTH, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -379,15 +504,24 @@ def main():
     r_e2e.render(scene, host_film)  # warm the host-film path
     torch.cuda.synchronize()
     e_rays = 0
+    e_samples = 0
     t0 = time.perf_counter()
     for i in range(args.e2e_steps):
         r_e2e.sample_offset = (i + 1) * n_step
         r_e2e.render(scene, host_film)
         e_rays += r_e2e.last_stats["extension_rays"] + r_e2e.last_stats["shadow_rays"]
+        e_samples += r_e2e.last_stats["camera_rays"]
     e_sec = time.perf_counter() - t0
-    e2e = {"value": e_rays / e_sec / 1e6, "unit": "Mrays/s",
+    e2e = {"value": e_rays / e_sec / 1e6, "unit": "Mrays/s", "msamples_per_s": e_samples / e_sec / 1e6,
            "h2d_bytes_per_step": ctypes_sizeof_params(), "d2h_bytes_per_step": WIDTH * HEIGHT * 3 * 8,
            "steps": args.e2e_steps}
+    scene.release_buffers()  # the measurements below render other scenes
+
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        torch.cuda.set_stream(torch.cuda.default_stream(dev))
+        extras["time_to_1pct"] = time_to_1pct(ng)
+        extras["adjoint"] = adjoint_cost(ng)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -409,8 +543,15 @@ def main():
             "msamples_per_s": all_samples / (ms / 1e3) / 1e6,
             "rays_per_sample": all_rays / max(all_samples, 1),
             "bvh_build_ms": info["bvh_build_ms"], "bvh_bytes": info["bvh_bytes"],
-            "roofline": roofline, "e2e": e2e, "gpu_launches": totals["launches"], "clocks": clocks.summary(),
+            "roofline": roofline, "roofline_logic": rl_logic, "e2e": e2e, "gpu_launches": totals["launches"],
+            "clocks": clocks.summary(),
         }
+        if extras:
+            t1 = extras["time_to_1pct"]
+            line["time_to_1pct_s"] = {"fp32": t1["fp32"]["seconds"], "fp64": t1["fp64"]["seconds"],
+                                      "fp64_over_fp32": t1["fp64_over_fp32"], "workload": t1["workload"]}
+            line["adjoint_over_forward"] = extras["adjoint"]["adjoint_over_forward"]
+            line["extras"] = extras
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -275,7 +275,7 @@ typedef struct ngi_batch_stats {
 } ngi_batch_stats;
 
 /* Renders num_jobs independent jobs -- scenes[i] with params[i] into the HOST film films[i]
- * (width*height*3 doubles, normalised as ngi_render does) -- through ONE persistent wave of
+ * (width*height*3 doubles, normalised as ngi_render does) -- through ONE shared wave of
  * path slots replayed from one CUDA graph: every job's samples share the slots, so small
  * jobs never leave the GPU idle. Jobs may differ in scene, renderer, resolution, samples,
  * max vertices and seed; all must use the same precision. The same scene handle may appear

@@ -464,6 +464,17 @@ __global__ void k_collapse_plan(BinView b, const WorkItem* __restrict__ work, in
     n_tri[w] = nt;
 }
 
+// Margin, in quanta, by which every quantised child plane other than the node origin lies outside
+// the child's box. The traversal decodes a plane at q quanta as q * (scale / d) + (origin - o) / d;
+// when the node origin is far from the ray origin along an axis the two terms nearly cancel and
+// the result carries an absolute error of a few float ulps of (origin - o) / d. A plane that fits
+// its child exactly (a child boundary on the quantum grid) could then be crossed a little early
+// and a box the ray enters be missed (seen on grazing rays off a 60-unit panel inside a
+// 1000-unit node). A 1/64-quantum margin exceeds that error while the ray origin lies within
+// ~300 node extents of the node origin along the axis; farther out the two terms do not cancel
+// and the relative padding of the box test covers the rounding.
+constexpr float kQuantMargin = 1.0f / 64.0f;
+
 // Emit: quantise, assign slots, write the node, gather leaf triangles, queue internal children.
 __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, int nwork,
                                 const uint32_t* __restrict__ children, const int* __restrict__ int_off,
@@ -491,9 +502,11 @@ __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, in
     uint32_t ebits[3];
     float inv_scale[3];
     const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
+    // Quantum per axis: a power of two at least ext / 254, so that a child's planes fit in 0..255
+    // with the margin below.
     for (int k = 0; k < 3; k++) {
         const float ext = __fsub_ru(h3[k], l3[k]);
-        const float s = __fdiv_ru(ext, 255.0f);
+        const float s = __fdiv_ru(ext, 254.0f);
         uint32_t bits = __float_as_uint(s);
         uint32_t e = (bits >> 23) & 0xFFu;
         if (bits & 0x7FFFFFu) e += 1;
@@ -551,8 +564,9 @@ __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, in
         const float cl[3] = {clo[c].x, clo[c].y, clo[c].z}, chh[3] = {chi[c].x, chi[c].y, chi[c].z};
         uint8_t ql[3], qh[3];
         for (int k = 0; k < 3; k++) {
-            const float a = floorf(__fsub_rd(cl[k], l3[k]) * inv_scale[k]);
-            const float bq = ceilf(__fsub_ru(chh[k], l3[k]) * inv_scale[k]);
+            // outward by at least kQuantMargin quanta (a plane at q = 0 is the node origin itself)
+            const float a = floorf(__fsub_rd(cl[k], l3[k]) * inv_scale[k] - kQuantMargin);
+            const float bq = ceilf(__fsub_ru(chh[k], l3[k]) * inv_scale[k] + kQuantMargin);
             ql[k] = (uint8_t)fminf(fmaxf(a, 0.0f), 255.0f);
             qh[k] = (uint8_t)fminf(fmaxf(bq, 0.0f), 255.0f);
         }

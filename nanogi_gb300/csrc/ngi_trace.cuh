@@ -86,7 +86,12 @@ constexpr int kTraversalStack = 64;
 // hot lines per lane already hit L1.
 
 // Relative padding of the box interval: keeps the box test conservative against the few
-// ulps of rounding in the slab distances (Ize, JCGT 2013).
+// ulps of rounding in the slab distances (Ize, JCGT 2013). The interval starts at 0 rather
+// than at the ray's tmin: the watertight t of a large triangle carries an absolute error of a
+// few ulps of its vertex coordinates, so at the reference's absolute tmin = 1e-4 a triangle
+// whose plane the ray crosses just below tmin can still test at t >= tmin (a surface point
+// reconstructed behind a 550-unit wall, say). The triangle test alone applies tmin, so a hit
+// does not depend on which boxes enclose the triangle.
 constexpr float kBoxLo = 1.0f - 1.0f / 1048576.0f;
 constexpr float kBoxHi = 1.0f + 1.0f / 1048576.0f;
 // tn Lo <= tf Hi as one product, tn <= tf (Hi / Lo): the same test for either sign of tn and tf
@@ -224,7 +229,8 @@ NGI_D uint32_t intersect_children(const CwNode* nodes, uint32_t idx, const TravS
             const float2 px = plane_pair(nearx, farx, j, make_float2(sx, sx), make_float2(ax, ax));
             const float2 py = plane_pair(neary, fary, j, make_float2(sy, sy), make_float2(ay, ay));
             const float2 pz = plane_pair(nearz, farz, j, make_float2(sz, sz), make_float2(az, az));
-            const float tn = fmaxf(fmaxf(px.x, py.x), fmaxf(pz.x, s.tmin));
+            // the interval starts at 0, not at tmin: tmin belongs to the triangle test alone
+            const float tn = fmaxf(fmaxf(px.x, py.x), fmaxf(pz.x, 0.0f));
             const float tf = fminf(fminf(px.y, py.y), fminf(pz.y, s.tmax));
             if (tn <= tf * kBoxRatio) hitmask |= ((child_bits4 >> (8 * j)) & 7u) << ((bit_index4 >> (8 * j)) & 31u);
         }

@@ -4,6 +4,7 @@
     python -m nanogi_gb300.studies adjoint
     python -m nanogi_gb300.studies batch
     python -m nanogi_gb300.studies precision [--ref-spp 1024]
+    python -m nanogi_gb300.studies fp32-error --workload terrain|batch|inverse [--spp 256] [--ref-spp 1024]
 
 convergence: time to reach 1% relative RMSE against an FP64 reference, for the tuned path
 (FP32 shading) and the plain path (FP64 shading and path state), `pt` on the Cornell-box
@@ -283,9 +284,106 @@ def batch(num_jobs: int = 256):
     return out
 
 
+def _blocks(x, b=16):
+    h, w = x.shape[:2]
+    y = x.sum(2)
+    return y[: h // b * b, : w // b * b].reshape(h // b, b, w // b, b).mean((1, 3))
+
+
+def _fp32_error(render, spp: int, ref_spp: int, blocks: int = 16):
+    """Error of the tuned FP32 path against an FP64 reference, with the noise taken out.
+
+    `render(precision, spp, seed, offset)` returns a normalised film. The reference is FP64 at
+    ref_spp in two independent halves (their difference gives its noise). FP32 and a second,
+    independent FP64 film are rendered at `spp`; on `blocks` x `blocks`-pixel block means
+    (where the per-pixel noise averages out) the FP64 film's error is the noise floor, and
+    the FP32 error beyond it, taken out in quadrature, is the bias FP32 adds."""
+    half = ref_spp // 2
+    ra = render("fp64", half, 9001, 0)
+    rb = render("fp64", half, 9001, half)
+    ref = 0.5 * (ra + rb)
+    sigma_ref_block = rel_rmse(_blocks(ra, blocks), _blocks(rb, blocks)) / 2.0
+    f32 = render("fp32", spp, 9101, 0)
+    f64 = render("fp64", spp, 9201, 0)
+    e32 = rel_rmse(_blocks(f32, blocks), _blocks(ref, blocks))
+    e64 = rel_rmse(_blocks(f64, blocks), _blocks(ref, blocks))
+    return {"spp": spp, "ref_spp": ref_spp, "block": blocks,
+            "block_rel_rmse_fp32": e32, "block_rel_rmse_fp64": e64, "reference_block_noise": sigma_ref_block,
+            "fp32_bias_beyond_noise": math.sqrt(max(e32 * e32 - e64 * e64, 0.0)),
+            "image_mean_ratio_fp32": float(f32.sum() / ref.sum()), "image_mean_ratio_fp64": float(f64.sum() / ref.sum()),
+            "pixel_rel_rmse_fp32": rel_rmse(f32, ref), "pixel_rel_rmse_fp64": rel_rmse(f64, ref)}
+
+
+def fp32_error(workload: str, spp: int = 256, ref_spp: int = 1024):
+    """FP32-against-FP64 error of one configuration (see _fp32_error):
+    terrain -- ptdirect 1920 x 1080, max length 16 (the headline workload);
+    batch   -- 16 jobs of the batched workload (each at its own resolution, path length and
+               materials; spp per job = `spp`), errors averaged over the jobs;
+    inverse -- the inverse-rendering box, ptdirect 512 x 512, max length 8, plus the relative
+               difference of the FP32 and FP64 path-replay gradients on the same paths."""
+    import nanogi_gb300 as ng
+    from nanogi_gb300 import scenegen
+
+    d = tempfile.mkdtemp(prefix="ngi_fp32err_")
+    if workload == "terrain":
+        w, h, m = 1920, 1080, 16
+        scene = ng.Scene.load(scenegen.write_scene(scenegen.terrain_scene(), d), w / h)
+
+        def render(precision, n, seed, offset):
+            return ng.Renderer(renderer="ptdirect", num_samples=w * h * n, max_num_vertices=m, width=w, height=h,
+                               seed=seed, sample_offset=w * h * offset, precision=precision).render(scene).copy()
+
+        out = {"workload": f"terrain_scene, {w}x{h}, ptdirect, max length {m}", **_fp32_error(render, spp, ref_spp)}
+        scene.close()
+        return out
+    if workload == "inverse":
+        w, h, m = 512, 512, 8
+        scene = ng.Scene.load(scenegen.write_scene(scenegen.inverse_box(seed=5, emitter_seed=7), d), w / h)
+
+        def render(precision, n, seed, offset):
+            return ng.Renderer(renderer="ptdirect", num_samples=w * h * n, max_num_vertices=m, width=w, height=h,
+                               seed=seed, sample_offset=w * h * offset, precision=precision).render(scene).copy()
+
+        out = {"workload": f"inverse_box, {w}x{h}, ptdirect, max length {m}", **_fp32_error(render, spp, ref_spp)}
+        # gradients of the same paths in both precisions (L2 loss against a zero image)
+        grads = {}
+        for precision in ("fp32", "fp64"):
+            r = ng.Renderer(renderer="ptdirect", num_samples=w * h * 64, max_num_vertices=m, width=w, height=h, seed=3,
+                            precision=precision)
+            img = r.render(scene)
+            grads[precision] = r.backward(scene, 2.0 * img)[0]
+        out["gradient_rel_diff_fp32_vs_fp64"] = rel_rmse(grads["fp32"], grads["fp64"])
+        scene.close()
+        return out
+    if workload == "batch":
+        pool, jobs = scenegen.batch_jobs(num_jobs=16)
+        paths = scenegen.write_batch(pool, jobs, d)
+        per_job = []
+        for path, j in zip(paths, jobs):
+            res = j["res"]
+            scene = ng.Scene.load(path, 1.0)
+
+            def render(precision, n, seed, offset, scene=scene, res=res, j=j):
+                return ng.Renderer(renderer="ptdirect", num_samples=res * res * n, max_num_vertices=j["max_vertices"],
+                                   width=res, height=res, seed=seed, sample_offset=res * res * offset,
+                                   precision=precision).render(scene).copy()
+
+            e = _fp32_error(render, spp, ref_spp, blocks=8 if res < 128 else 16)
+            e["res"], e["max_vertices"], e["triangles"] = res, j["max_vertices"], j["triangles"]
+            per_job.append(e)
+            scene.close()
+        keys = ("block_rel_rmse_fp32", "block_rel_rmse_fp64", "fp32_bias_beyond_noise", "image_mean_ratio_fp32")
+        return {"workload": "16 jobs of the batched workload, ptdirect", "jobs": per_job,
+                "mean": {k: float(np.mean([e[k] for e in per_job])) for k in keys},
+                "max_bias_beyond_noise": float(max(e["fp32_bias_beyond_noise"] for e in per_job))}
+    raise ValueError(workload)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["convergence", "adjoint", "batch", "precision"])
+    ap.add_argument("study", choices=["convergence", "adjoint", "batch", "precision", "fp32-error"])
+    ap.add_argument("--workload", default="terrain", choices=["terrain", "batch", "inverse"])
+    ap.add_argument("--spp", type=int, default=256)
     ap.add_argument("--triangles", type=int, default=10_000_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--ref-spp", type=int, default=None)
@@ -299,6 +397,8 @@ def main():
         print(json.dumps(batch()), flush=True)
     elif a.study == "precision":
         print(json.dumps(precision(a.ref_spp or 1024, a.res, a.res, num_triangles=a.triangles)), flush=True)
+    elif a.study == "fp32-error":
+        print(json.dumps(fp32_error(a.workload, a.spp, a.ref_spp or 1024)), flush=True)
 
 
 if __name__ == "__main__":

@@ -224,8 +224,12 @@ struct Bvh {
     std::vector<int> order;
 };
 
+// Box test over [0, tbest]: the ray's tmin is applied by the triangle test alone, so the BVH finds
+// every hit the brute force finds (a triangle test can put t above tmin for a triangle whose
+// plane the ray crosses just below it: the test's rounding scales with the vertex coordinates).
 bool BoxTest(const RayF& r, const BNode& n, float tmin, float tbest) {
-    float tn = tmin, tf = tbest;
+    (void)tmin;
+    float tn = 0.0f, tf = tbest;
     for (int k = 0; k < 3; k++) {
         float a = (n.lo[k] - r.o[k]) * r.inv[k];
         float b = (n.hi[k] - r.o[k]) * r.inv[k];

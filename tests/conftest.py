@@ -52,12 +52,27 @@ def rel_rmse(a: np.ndarray, b: np.ndarray) -> float:
 def welch_z(gpu_films: np.ndarray, oracle_films: np.ndarray):
     """Per-pixel Welch z-scores of the mean of K independent GPU films against the mean of K
     independent oracle films (same expectation, different random numbers), over the pixels
-    where either side has variance. Returns (z, ratio of the image sums)."""
+    where either side has variance, and the same z-score for the image sum (every film's
+    total, one value per film). Returns (per-value z, image-sum z, ratio of the mean sums)."""
     K1, K2 = len(gpu_films), len(oracle_films)
     mg, mo = gpu_films.mean(0), oracle_films.mean(0)
     se = np.sqrt(gpu_films.var(0, ddof=1) / K1 + oracle_films.var(0, ddof=1) / K2)
     ok = se > 0
-    return (mg[ok] - mo[ok]) / se[ok], float(mg.sum() / max(mo.sum(), 1e-300))
+    sg, so = gpu_films.reshape(K1, -1).sum(1), oracle_films.reshape(K2, -1).sum(1)
+    se_sum = np.sqrt(sg.var(ddof=1) / K1 + so.var(ddof=1) / K2)
+    z_sum = float((sg.mean() - so.mean()) / se_sum) if se_sum > 0 else 0.0
+    return (mg[ok] - mo[ok]) / se[ok], z_sum, float(sg.mean() / max(so.mean(), 1e-300))
+
+
+def assert_same_expectation(gpu_films: np.ndarray, oracle_films: np.ndarray, label: str = "") -> None:
+    """GPU and oracle films estimate the same image: the per-value z-scores look like noise
+    (mean near 0, few beyond 4) and the image sums agree within 4 standard errors."""
+    z, z_sum, ratio = welch_z(gpu_films, oracle_films)
+    print(f"{label}: z mean {z.mean():+.3f}, |z|>4 share {(np.abs(z) > 4).mean():.4f}, image-sum z {z_sum:+.2f}, "
+          f"ratio {ratio:.4f}")
+    assert abs(z.mean()) < 0.15, (label, z.mean())
+    assert (np.abs(z) > 4.0).mean() < 0.01, label
+    assert abs(z_sum) < 4.0, (label, z_sum)
 
 
 def camera_rays(desc, n: int, aspect: float, rng, tmin: float = 1e-4) -> np.ndarray:
@@ -106,11 +121,12 @@ T_REL_TOL = 1e-5  # hit-distance tolerance
 def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999):
     """First hits of the GPU traversal against the oracle's for the same rays.
 
-    Hit / miss agree; primitive ids are bit-exact on every ray whose nearest hit is not a tie
-    (two triangles at the identical distance, where traversal order picks one: there the
-    distances must still be identical); hit distances are within T_REL_TOL everywhere and
-    bit-identical on at least `min_exact` of the rays; barycentrics agree to 1e-6.
-    Returns (hit rays compared, ties) for reporting."""
+    Hit / miss agree and primitive ids are bit-exact, except on ties: rays whose two answers lie
+    at the same distance to within T_REL_TOL (coincident surfaces, such as a box standing on a
+    floor or two triangles sharing the edge the ray hits, where the watertight test's rounding or
+    the traversal order picks one of them); ties must stay below `max_tie_share`. Hit distances
+    are within T_REL_TOL everywhere and bit-identical on at least `min_exact` of the rays where
+    the ids agree; barycentrics agree to 1e-6 there. Returns (hit rays compared, ties)."""
     gp, gt, guv = gpu
     op, ot, ouv = ora
     miss_agree = (gp < 0) == (op < 0)
@@ -118,10 +134,12 @@ def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999):
     both = (gp >= 0) & (op >= 0)
     same = gp[both] == op[both]
     tie = ~same
-    assert np.array_equal(gt[both][tie], ot[both][tie]), f"{label}: primitive ids differ on non-tie rays"
-    assert tie.mean() <= max_tie_share, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
     rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
-    assert rel.max() <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
+    bad = tie & (rel > T_REL_TOL)
+    assert not bad.any(), (f"{label}: {bad.sum()} rays hit different primitives at different distances, e.g. "
+                           f"gpu t={gt[both][bad][:3]} oracle t={ot[both][bad][:3]}")
+    assert tie.mean() <= max_tie_share, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
+    assert rel.max(initial=0.0) <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
     exact = (gt[both][same] == ot[both][same]).mean() if same.any() else 1.0
     assert exact >= min_exact, f"{label}: only {exact:.6f} of hit distances are bit-identical"
     if same.any():

@@ -13,7 +13,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import rel_rmse
+from conftest import assert_same_expectation, rel_rmse
 
 pytestmark = pytest.mark.gpu
 
@@ -42,14 +42,7 @@ def test_statistical_parity_with_reference_sampling(native_lib, cornell, rendere
                      seed=100 + k).render(scene) for k in range(K)])
     o = np.stack([ora.render(renderer, num_samples=W * H * spp, max_vertices=8, width=W, height=H, seed=200 + k,
                              rng_mode="reference") for k in range(K)])
-    mg, mo = g.mean(0), o.mean(0)
-    se = np.sqrt(g.var(0, ddof=1) / K + o.var(0, ddof=1) / K)
-    ok = se > 0
-    z = (mg[ok] - mo[ok]) / se[ok]
-    assert abs(z.mean()) < 0.15, z.mean()
-    assert (np.abs(z) > 4.0).mean() < 0.01
-    # the whole image agrees far better than any single pixel
-    assert abs(mg.sum() / mo.sum() - 1) < 0.02
+    assert_same_expectation(g, o, f"cornell {renderer}")
 
 
 @pytest.mark.parametrize("renderer", ["pt", "ptdirect"])
