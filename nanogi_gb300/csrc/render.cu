@@ -65,12 +65,11 @@ struct WaveCounters {
     int sh_count;
     int active;
     int ext_fetch;                    // rays handed out by the persistent traversal kernel
-    int sh_fetch;                     // unused (kept for the layout)
+    int sh_fetch;                     // rays handed out by the shadow-only traversal kernel
+    int regen_count;                  // slots handed from path shading to regeneration
     int error_flags;                  // bit 0: traversal stack overflow
-    // compacted shading: the hit, regeneration and carry queues, double-buffered by iteration parity
-    int hit_count[2];
-    int regen_count[2];
-    int carry_count[2];
+    int ext_count_b;                  // compacted shading: count of the second extension queue
+    int carry_count[2];               //   and of the two carry queues (reset per iteration by parity)
     unsigned long long stat_camera;
     unsigned long long stat_ext;
     unsigned long long stat_shadow;
@@ -118,27 +117,16 @@ struct WaveView {
     uint8_t* state;
     int* ext_queue;          // the iteration's extension rays (slot ids), traced by k_trace
     int* ext_count;          // their number (a counter in ctr)
-    // compacted shading (ptdirect), queues double-buffered by iteration parity and set per
-    // iteration: the traversal sends each finished extension ray's slot to the next iteration's
-    // hit queue or, when it hit nothing (the path ends), to its regeneration queue; shading reads
-    // the hit queue and the slots regeneration left empty (carry), and appends the paths that end
-    // to the regeneration queue, which regeneration then reads
-    const int* hit_in;
-    const int* hit_in_count;
-    int* hit_out;            // null: not compacted, the traversal only writes the hit record
-    int* hit_out_count;
-    int* miss_out;
-    int* miss_out_count;
-    int* regen_queue;
-    int* regen_count;
+    int* regen_queue;        // slots whose path ended this iteration (split path logic)
+    // compacted shading (ptdirect): the slots to shade are the previous iteration's extension
+    // queue and the slots regeneration left empty; both are double-buffered by iteration parity
+    const int* ext_in;
+    const int* ext_in_count;
     const int* carry_in;
     const int* carry_in_count;
     int* carry_out;
     int* carry_out_count;
-    int* hit_a;              // storage of the double-buffered queues
-    int* hit_b;
-    int* regen_a;
-    int* regen_b;
+    int* ext_queue_b;        // the second extension-queue buffer and the two carry buffers
     int* carry_a;
     int* carry_b;
     float4* sh_o;
@@ -581,8 +569,8 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
     // of the block size). n_items is the same for every thread of a block, so all of them run the
     // same iterations.
     // (every queue holds at most one entry per slot; the clamps only keep a corrupted count in bounds)
-    const int n_ext_in = PART == kLogicShadeQ ? min(*w.hit_in_count, w.Q) : 0;
-    const int n_items = PART == kLogicRegen    ? min(*w.regen_count, w.Q)
+    const int n_ext_in = PART == kLogicShadeQ ? min(*w.ext_in_count, w.Q) : 0;
+    const int n_items = PART == kLogicRegen    ? min(w.ctr->regen_count, w.Q)
                         : PART == kLogicShadeQ ? n_ext_in + min(*w.carry_in_count, w.Q - n_ext_in)
                                                : w.Q;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += stride) {
@@ -594,7 +582,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             s = valid ? w.regen_queue[item] : 0;
             st = SLOT_EMPTY;
         } else if (PART == kLogicShadeQ) {
-            s = !valid ? 0 : (item < n_ext_in ? w.hit_in[item] : w.carry_in[item - n_ext_in]);
+            s = !valid ? 0 : (item < n_ext_in ? w.ext_in[item] : w.carry_in[item - n_ext_in]);
             st = !valid ? (uint8_t)SLOT_DONE : (item < n_ext_in ? (uint8_t)SLOT_ACTIVE : (uint8_t)SLOT_EMPTY);
         } else {
             st = w.state[s];
@@ -691,7 +679,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
 
         if (PART == kLogicShadeQ) {
             // ---- hand the slots whose path ended to the regeneration kernel ----
-            const int q = warp_append(w.regen_count, need_new);
+            const int q = warp_append(&w.ctr->regen_count, need_new);
             if (need_new) w.regen_queue[q] = s;
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
@@ -1330,7 +1318,6 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
     uint2 stack[kTraversalStack];
     int item = -1, slot = -1, job = 0;
     bool shadow = false;
-    bool pending = false;  // compacted shading: this lane's finished extension ray awaits its queue append
     const CwNode* nodes = sv.nodes;
     const float4* tris = sv.tris;
     int num_nodes = sv.num_nodes;
@@ -1344,19 +1331,7 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
     while (true) {
         const bool idle = item < 0;
         const unsigned idle_mask = __ballot_sync(0xFFFFFFFFu, idle);
-        const bool refill_now = !exhausted && __popc(idle_mask) >= refill;
-        if (w.hit_out && (refill_now || idle_mask == 0xFFFFFFFFu)) {
-            // compacted shading: the warp's finished extension rays go to the next iteration's hit
-            // queue, or, when they hit nothing (the path ends), to its regeneration queue -- one
-            // atomic per queue for all of them, before the refill reuses their lanes
-            const bool h = pending && s.hit >= 0, m = pending && s.hit < 0;
-            const int qh = warp_append(w.hit_out_count, h);
-            if (h) w.hit_out[qh] = slot;
-            const int qm = warp_append(w.miss_out_count, m);
-            if (m) w.miss_out[qm] = slot;
-            pending = false;
-        }
-        if (refill_now) {
+        if (!exhausted && __popc(idle_mask) >= refill) {
             const int leader = __ffs(idle_mask) - 1;
             int base = 0;
             if ((int)lane_id() == leader) base = atomicAdd(fetch, __popc(idle_mask));
@@ -1416,10 +1391,6 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
                             atomicAdd(&w.ctr->stat_nonfinite, 1ull);  // rare: no register kept for it
                         }
                     }
-                } else if (w.hit_out) {
-                    // compacted shading: the queue append waits for the warp's next refill
-                    if (s.hit >= 0) w.hit[slot] = make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit));
-                    pending = true;
                 } else {
                     w.hit[slot] = make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit));
                 }
@@ -1701,16 +1672,6 @@ void RequireSceneDevice(const DeviceScene& ds) {
 // ---- render driver ------------------------------------------------------------------------------
 namespace {
 
-// Queues of compacted shading: chosen per iteration by enqueue_iteration, null otherwise.
-template <typename R>
-void clear_compact_queues(WaveView<R>& v) {
-    v.hit_in = v.hit_in_count = nullptr;
-    v.hit_out = v.hit_out_count = v.miss_out = v.miss_out_count = nullptr;
-    v.regen_queue = v.regen_count = nullptr;
-    v.carry_in = v.carry_in_count = nullptr;
-    v.carry_out = v.carry_out_count = nullptr;
-}
-
 template <typename R>
 void alloc_wave_view(RenderWave* wv, WaveView<R>& v, int Q) {
     auto A = [&](size_t bytes) -> void* {
@@ -1735,19 +1696,18 @@ void alloc_wave_view(RenderWave* wv, WaveView<R>& v, int Q) {
     v.nverts = (int*)A(sizeof(int) * Q);
     v.state = (uint8_t*)A(sizeof(uint8_t) * Q);
     v.ext_queue = (int*)A(sizeof(int) * Q);
-    v.hit_a = (int*)A(sizeof(int) * Q);
-    v.hit_b = (int*)A(sizeof(int) * Q);
-    v.regen_a = (int*)A(sizeof(int) * Q);
-    v.regen_b = (int*)A(sizeof(int) * Q);
+    v.ext_queue_b = (int*)A(sizeof(int) * Q);
     v.carry_a = (int*)A(sizeof(int) * Q);
     v.carry_b = (int*)A(sizeof(int) * Q);
+    v.regen_queue = (int*)A(sizeof(int) * Q);
     v.sh_o = (float4*)A(sizeof(float4) * kShadowPerSlot * (size_t)Q);
     v.sh_d = (float4*)A(sizeof(float4) * kShadowPerSlot * (size_t)Q);
     v.sh_c = (Vec4T<R>*)A(sizeof(Vec4T<R>) * kShadowPerSlot * (size_t)Q);
     v.sh_pix = (uint32_t*)A(sizeof(uint32_t) * kShadowPerSlot * (size_t)Q);
     v.ctr = wv->ctr;
     v.ext_count = &v.ctr->ext_count;
-    clear_compact_queues(v);
+    v.ext_in = v.ext_in_count = v.carry_in = v.carry_in_count = nullptr;  // set per iteration when compacted
+    v.carry_out = v.carry_out_count = nullptr;
 }
 
 RenderWave* ensure_wave_exact(DeviceScene& ds, int Q, int precision) {
@@ -1820,7 +1780,13 @@ int trace_grid() {
     return g;
 }
 
-// Compacted shading applies to ptdirect's camera paths outside batches.
+// Compacted shading applies to ptdirect's camera paths outside batches. Measured and not kept:
+// the traversal sending each finished extension ray's slot either to a hit queue for shading or,
+// on a miss, straight to the next regeneration queue (43.6% of the terrain's extension rays
+// miss), with the appends batched per warp at each refill. Shading visited only hits, but the
+// logic kernels' time per iteration stayed at 0.34 ms (a miss costs shading little: one hit
+// record read and a queue append), while the traversal launch grew from 0.613 to 0.644 ms:
+// 1741 against 1791 Mrays/s on the terrain.
 template <bool DIRECT, bool BATCH, int LOGIC>
 constexpr bool compact_shading() {
     return DIRECT && !BATCH && LOGIC == kLogicCamera;
@@ -1830,13 +1796,13 @@ constexpr bool compact_shading() {
 // the ones it reads (filled by the previous iteration) keep their counts.
 __global__ void k_iteration_begin(WaveCounters* ctr, int parity) {
     if (threadIdx.x != 0) return;
-    ctr->ext_count = 0;
     ctr->sh_count = 0;
     ctr->active = 0;
     ctr->ext_fetch = 0;
     ctr->sh_fetch = 0;
-    ctr->hit_count[1 - parity] = 0;
-    ctr->regen_count[1 - parity] = 0;
+    ctr->regen_count = 0;
+    if (parity) ctr->ext_count = 0;
+    else ctr->ext_count_b = 0;
     ctr->carry_count[1 - parity] = 0;
 }
 
@@ -1855,17 +1821,14 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
     constexpr bool compact = compact_shading<DIRECT, BATCH, LOGIC>();
     WaveView<R> vq = v;
     if constexpr (compact) {
-        // parity p shades hit queue p and carry queue p and regenerates regeneration queue p; its
-        // traversal fills hit queue 1-p and regeneration queue 1-p (misses), its regeneration
-        // carry queue 1-p
-        vq.hit_in = parity ? v.hit_b : v.hit_a;
-        vq.hit_in_count = &ctr->hit_count[parity];
-        vq.hit_out = parity ? v.hit_a : v.hit_b;
-        vq.hit_out_count = &ctr->hit_count[1 - parity];
-        vq.regen_queue = parity ? v.regen_b : v.regen_a;
-        vq.regen_count = &ctr->regen_count[parity];
-        vq.miss_out = parity ? v.regen_a : v.regen_b;
-        vq.miss_out_count = &ctr->regen_count[1 - parity];
+        // parity p reads extension queue p and carry queue p, fills extension queue 1-p (traced
+        // this iteration) and carry queue 1-p
+        int* const cnt_e0 = &ctr->ext_count;
+        int* const cnt_e1 = &ctr->ext_count_b;
+        vq.ext_in = parity ? v.ext_queue_b : v.ext_queue;
+        vq.ext_in_count = parity ? cnt_e1 : cnt_e0;
+        vq.ext_queue = parity ? v.ext_queue : v.ext_queue_b;
+        vq.ext_count = parity ? cnt_e0 : cnt_e1;
         vq.carry_in = parity ? v.carry_b : v.carry_a;
         vq.carry_in_count = &ctr->carry_count[parity];
         vq.carry_out = parity ? v.carry_a : v.carry_b;
@@ -2572,7 +2535,6 @@ size_t carve_wave(unsigned char* base, int Q, WaveView<R>& v) {
     v.Q = Q;
     v.ctr = (WaveCounters*)take(sizeof(WaveCounters));
     v.ext_count = v.ctr ? &v.ctr->ext_count : nullptr;
-    clear_compact_queues(v);
     v.ray_o = (float4*)take(sizeof(float4) * Q);
     v.ray_d = (float4*)take(sizeof(float4) * Q);
     v.hit = (float4*)take(sizeof(float4) * Q);
@@ -2588,12 +2550,10 @@ size_t carve_wave(unsigned char* base, int Q, WaveView<R>& v) {
     v.nverts = (int*)take(sizeof(int) * Q);
     v.state = (uint8_t*)take(sizeof(uint8_t) * Q);
     v.ext_queue = (int*)take(sizeof(int) * Q);
-    v.hit_a = (int*)take(sizeof(int) * Q);
-    v.hit_b = (int*)take(sizeof(int) * Q);
-    v.regen_a = (int*)take(sizeof(int) * Q);
-    v.regen_b = (int*)take(sizeof(int) * Q);
+    v.ext_queue_b = (int*)take(sizeof(int) * Q);
     v.carry_a = (int*)take(sizeof(int) * Q);
     v.carry_b = (int*)take(sizeof(int) * Q);
+    v.regen_queue = (int*)take(sizeof(int) * Q);
     v.sh_o = (float4*)take(sizeof(float4) * kShadowPerSlot * (size_t)Q);
     v.sh_d = (float4*)take(sizeof(float4) * kShadowPerSlot * (size_t)Q);
     v.sh_c = (Vec4T<R>*)take(sizeof(Vec4T<R>) * kShadowPerSlot * (size_t)Q);
