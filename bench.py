@@ -24,6 +24,8 @@ Reported (one JSON line on rank 0):
              fit (reference: FP64 at 16,384 spp in two halves, its noise subtracted)
   adjoint    the metric's third part: path-replay backward time over forward time (ptdirect,
              512 x 512, 64 spp, 64 diffuse material groups)
+  interior   Mrays/s on the ~10M-triangle precision interior (ptdirect 1024 x 1024, max length 32),
+             the configuration whose BVH and triangles exceed L2
   cpu_baseline  the CPU oracle (the reference's algorithm restated, FP64, mt19937 stream)
              on this host's cores over a bounded sample of the same workload
 `--impl reference` times that CPU implementation alone, with all host threads.
@@ -335,6 +337,45 @@ def adjoint_cost(ng, w=512, h=512, spp=64, m=8, repeats=5):
             "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd}
 
 
+def interior_throughput(ng, steps=4, spp=16, w=1024, h=1024, m=32):
+    """Mrays/s and Msamples/s of the ~10M-triangle precision interior (ptdirect, FP32 shading,
+    scaled ray offsets), device time of `steps` renders of `spp` samples per pixel each."""
+    from nanogi_gb300 import scenegen
+
+    t0 = time.perf_counter()
+    desc = scenegen.precision_interior()
+    d = tempfile.mkdtemp(prefix="ngi_interior_")
+    scene = ng.Scene.load_with_meshes(scenegen.write_scene(desc, d, write_meshes=False), w / h,
+                                      scenegen.memory_meshes(desc))
+    del desc
+    scene.build()
+    setup_s = time.perf_counter() - t0
+    info = scene.info()
+
+    def render(offset, flags=0):
+        r = ng.Renderer(renderer="ptdirect", num_samples=w * h * spp, max_num_vertices=m, width=w, height=h, seed=77,
+                        sample_offset=offset, precision="fp32", ray_offset="scaled", flags=flags)
+        r.render(scene)
+        return r.last_stats
+
+    render(0)
+    ms = rays = samples = 0
+    for i in range(steps):
+        st = render((i + 1) * w * h * spp)
+        ms += st["render_ms"]
+        rays += st["extension_rays"] + st["shadow_rays"]
+        samples += st["camera_rays"]
+    st = render(0, flags=ng.capi.TRAVERSAL_COUNTERS)
+    scene.close()
+    return {"workload": f"precision_interior {info['num_triangles']} tris, {w}x{h}, ptdirect, max length {m}, "
+                        f"{spp} spp per step, scaled ray offsets",
+            "mrays_per_s": rays / (ms / 1e3) / 1e6, "msamples_per_s": samples / (ms / 1e3) / 1e6,
+            "steps": steps, "ms_per_step": ms / steps, "bvh_build_ms": info["bvh_build_ms"],
+            "bvh_bytes": info["bvh_bytes"], "setup_seconds": setup_s,
+            "nodes_per_extension_ray": st["extend_nodes"] / max(st["extension_rays"], 1),
+            "tris_per_extension_ray": st["extend_tris"] / max(st["extension_rays"], 1)}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -522,6 +563,8 @@ def main():
         torch.cuda.set_stream(torch.cuda.default_stream(dev))
         extras["time_to_1pct"] = time_to_1pct(ng)
         extras["adjoint"] = adjoint_cost(ng)
+        if WORKLOAD == "terrain":
+            extras["interior"] = interior_throughput(ng)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -551,6 +594,8 @@ def main():
             line["time_to_1pct_s"] = {"fp32": t1["fp32"]["seconds"], "fp64": t1["fp64"]["seconds"],
                                       "fp64_over_fp32": t1["fp64_over_fp32"], "workload": t1["workload"]}
             line["adjoint_over_forward"] = extras["adjoint"]["adjoint_over_forward"]
+            if "interior" in extras:
+                line["interior_mrays_per_s"] = extras["interior"]["mrays_per_s"]
             line["extras"] = extras
         if cpu:
             line["cpu_baseline"] = cpu

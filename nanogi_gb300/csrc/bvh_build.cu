@@ -2,15 +2,20 @@
 //
 // Replaces the Embree build of include/nanogi/rt.hpp:2087-2143. Pipeline (all on device):
 //   1. per-triangle bounds and centroid bounds
-//   2. 63-bit Morton codes of the centroids, radix sort (CUB)
-//   3. binary tree: PLOC clustering of the sorted leaves (Meister and Bittner 2018), leaves
+//   2. pre-splitting (Ernst and Greiner 2007; Karras and Aila 2013): a triangle whose box is
+//      far larger than the triangle itself (a long thin strip lying diagonally) becomes several
+//      references, the triangle clipped to slabs of its box, each with the tight box of its
+//      part; every other triangle is one reference
+//   3. 63-bit Morton codes of the reference box centroids, radix sort (CUB)
+//   4. binary tree: PLOC clustering of the sorted leaves (Meister and Bittner 2018), leaves
 //      renumbered depth-first so every subtree is a contiguous range
-//   4. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017): a
+//   5. top-down, level-synchronous collapse into 8-wide nodes (Ylitie et al. 2017): a
 //      bottom-up pass finds the SAH-optimal way to write every subtree as at most 1..8
 //      roots, and each node opens its binary descendants as that minimum says; subtrees of
 //      <= 3 triangles become leaves, children are assigned to slots by ray octant, and child
 //      boxes are quantised to 8 bits per plane relative to the parent.
-//   5. triangles, normals and uvs are gathered into leaf order.
+//   6. triangles, normals and uvs are gathered into leaf order (a split triangle once per leaf
+//      holding one of its references; the watertight test always runs on the whole triangle).
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -112,6 +117,150 @@ __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict
     }
     keys[i] = (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
     vals[i] = (uint32_t)i;
+}
+
+// ---- pre-splitting -----------------------------------------------------------------------------
+// A triangle is split when the surface area of its box exceeds kSplitRatio times its own area
+// (a flat triangle lying in an axis plane has a ratio of 4, a typical mesh triangle 4-10), into
+// min(kMaxPieces, ratio / kSplitRatio) references; the extra references of a scene are capped at
+// kSplitBudget times its triangle count by scaling every request down. Each reference is the
+// triangle clipped to one of equal slabs along the longest axis of its box: for a long thin
+// diagonal triangle the k pieces' boxes add up to about 1/k of the whole box's area.
+constexpr float kSplitRatio = 16.0f;
+constexpr uint32_t kMaxPieces = 64;
+constexpr double kSplitBudget = 1.0;
+
+__global__ void k_split_counts(const float* __restrict__ pos, const float4* __restrict__ lo,
+                               const float4* __restrict__ hi, int n, uint32_t* __restrict__ pieces,
+                               unsigned long long* __restrict__ extra) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t k = 1;
+    if (i < n) {
+        const float* p = pos + 9 * (size_t)i;
+        const double ax = (double)p[3] - p[0], ay = (double)p[4] - p[1], az = (double)p[5] - p[2];
+        const double bx = (double)p[6] - p[0], by = (double)p[7] - p[1], bz = (double)p[8] - p[2];
+        const double cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+        const double area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+        const double dx = (double)hi[i].x - lo[i].x, dy = (double)hi[i].y - lo[i].y, dz = (double)hi[i].z - lo[i].z;
+        const double box = 2.0 * (dx * dy + dy * dz + dz * dx);
+        if (area > 0.0 && box > kSplitRatio * area)
+            k = (uint32_t)fmin((double)kMaxPieces, floor(box / (kSplitRatio * area)));
+        pieces[i] = k;
+    }
+    // warp sum of the extra references, one atomic per warp
+    unsigned long long e = k - 1;
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+    if ((threadIdx.x & 31) == 0 && e) atomicAdd(extra, e);
+}
+
+// Scales every triangle's extra references by `scale` (< 1) to keep within the budget.
+__global__ void k_split_scale(uint32_t* __restrict__ pieces, int n, double scale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pieces[i] = 1u + (uint32_t)floor((double)(pieces[i] - 1u) * scale);
+}
+
+// Sutherland-Hodgman clip of a convex polygon (x, y, z per vertex) against coordinate `axis`
+// >= v (keep_ge) or <= v; the cut points get the plane coordinate exactly.
+__device__ int clip_polygon(const double (*in)[3], int nin, double (*out)[3], int axis, double v, bool keep_ge) {
+    int nout = 0;
+    for (int a = 0; a < nin; a++) {
+        const int b = a + 1 == nin ? 0 : a + 1;
+        const double da = keep_ge ? in[a][axis] - v : v - in[a][axis];
+        const double db = keep_ge ? in[b][axis] - v : v - in[b][axis];
+        if (da >= 0.0) {
+            for (int k = 0; k < 3; k++) out[nout][k] = in[a][k];
+            nout++;
+        }
+        if ((da >= 0.0) != (db >= 0.0)) {
+            const double t = da / (da - db);
+            for (int k = 0; k < 3; k++) out[nout][k] = in[a][k] + t * (in[b][k] - in[a][k]);
+            out[nout][axis] = v;
+            nout++;
+        }
+    }
+    return nout;
+}
+
+// Writes the references of every triangle: its box, or the boxes of its slab pieces, rounded
+// outward to float and clamped to the triangle's own box; ref_tri[r] = the triangle of r.
+__global__ void k_split_emit(const float* __restrict__ pos, const float4* __restrict__ lo,
+                             const float4* __restrict__ hi, int n, const uint32_t* __restrict__ pieces,
+                             const uint32_t* __restrict__ first, float4* __restrict__ ref_lo,
+                             float4* __restrict__ ref_hi, uint32_t* __restrict__ ref_tri) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = pieces[i], base = first[i];
+    const float4 l = lo[i], h = hi[i];
+    if (k <= 1) {
+        ref_lo[base] = l;
+        ref_hi[base] = h;
+        ref_tri[base] = (uint32_t)i;
+        return;
+    }
+    const float ext[3] = {h.x - l.x, h.y - l.y, h.z - l.z};
+    const int axis = ext[0] >= ext[1] ? (ext[0] >= ext[2] ? 0 : 2) : (ext[1] >= ext[2] ? 1 : 2);
+    const double a0 = axis == 0 ? l.x : (axis == 1 ? l.y : l.z);
+    const double a1 = axis == 0 ? h.x : (axis == 1 ? h.y : h.z);
+    const float* p = pos + 9 * (size_t)i;
+    double tri[3][3];
+    for (int v = 0; v < 3; v++)
+        for (int c = 0; c < 3; c++) tri[v][c] = p[3 * v + c];
+    for (uint32_t j = 0; j < k; j++) {
+        // adjacent pieces share the same boundary value, so the pieces cover the triangle
+        const double s0 = j == 0 ? a0 : a0 + (a1 - a0) * (double)j / (double)k;
+        const double s1 = j + 1 == k ? a1 : a0 + (a1 - a0) * (double)(j + 1) / (double)k;
+        double q1[5][3], q2[5][3];
+        const int n1 = clip_polygon(tri, 3, q1, axis, s0, true);
+        const int n2 = clip_polygon(q1, n1, q2, axis, s1, false);
+        double bl[3] = {1e300, 1e300, 1e300}, bh[3] = {-1e300, -1e300, -1e300};
+        for (int v = 0; v < n2; v++)
+            for (int c = 0; c < 3; c++) {
+                bl[c] = fmin(bl[c], q2[v][c]);
+                bh[c] = fmax(bh[c], q2[v][c]);
+            }
+        float4 rl = l, rh = h;
+        if (n2 > 0) {
+            rl = make_float4(fmaxf(__double2float_rd(bl[0]), l.x), fmaxf(__double2float_rd(bl[1]), l.y),
+                             fmaxf(__double2float_rd(bl[2]), l.z), 0.0f);
+            rh = make_float4(fminf(__double2float_ru(bh[0]), h.x), fminf(__double2float_ru(bh[1]), h.y),
+                             fminf(__double2float_ru(bh[2]), h.z), 0.0f);
+        }
+        ref_lo[base + j] = rl;
+        ref_hi[base + j] = rh;
+        ref_tri[base + j] = (uint32_t)i;
+    }
+}
+
+// Bounds of the reference box centroids (the Morton grid).
+__global__ void k_centroid_bounds(const float4* __restrict__ lo, const float4* __restrict__ hi, int n,
+                                  int* __restrict__ cbounds) {
+    __shared__ int smin[3][32], smax[3][32];
+    int cmin[3] = {INT_MAX, INT_MAX, INT_MAX}, cmax[3] = {INT_MIN, INT_MIN, INT_MIN};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 l = lo[i], h = hi[i];
+        const float c[3] = {0.5f * (l.x + h.x), 0.5f * (l.y + h.y), 0.5f * (l.z + h.z)};
+        for (int k = 0; k < 3; k++) {
+            const int o = float_to_ordered(c[k]);
+            cmin[k] = min(cmin[k], o);
+            cmax[k] = max(cmax[k], o);
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            cmin[k] = min(cmin[k], __shfl_xor_sync(0xFFFFFFFFu, cmin[k], o));
+            cmax[k] = max(cmax[k], __shfl_xor_sync(0xFFFFFFFFu, cmax[k], o));
+        }
+        if (lane == 0) { smin[k][warp] = cmin[k]; smax[k][warp] = cmax[k]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        int a = INT_MAX, b = INT_MIN;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a = min(a, smin[k][w]); b = max(b, smax[k][w]); }
+        atomicMin(&cbounds[k], a);
+        atomicMax(&cbounds[3 + k], b);
+    }
 }
 
 // ---- PLOC: parallel locally-ordered clustering (Meister and Bittner, TVCG 2018) --------------
@@ -479,9 +628,10 @@ constexpr float kQuantMargin = 1.0f / 64.0f;
 __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, int nwork,
                                 const uint32_t* __restrict__ children, const int* __restrict__ int_off,
                                 const int* __restrict__ tri_off, uint32_t node_base, uint32_t tri_base_all,
-                                const uint32_t* __restrict__ sorted_tri, const float* __restrict__ pos,
-                                CwNode* __restrict__ nodes, float4* __restrict__ tris_out,
-                                uint32_t* __restrict__ perm, WorkItem* __restrict__ next_work) {
+                                const uint32_t* __restrict__ sorted_tri, const uint32_t* __restrict__ ref_tri,
+                                const float* __restrict__ pos, CwNode* __restrict__ nodes,
+                                float4* __restrict__ tris_out, uint32_t* __restrict__ perm,
+                                WorkItem* __restrict__ next_work) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nwork) return;
     uint32_t ch[8];
@@ -584,7 +734,7 @@ __global__ void k_collapse_emit(BinView b, const WorkItem* __restrict__ work, in
             node.meta[s] = (uint8_t)((unary << 5) | (uint32_t)tri_rank);
             const int first = ref_first(b, r);
             for (int q = 0; q < cnt; q++) {
-                const uint32_t tri = sorted_tri[first + q];
+                const uint32_t tri = ref_tri[sorted_tri[first + q]];
                 const uint32_t dst = tri_base + (uint32_t)tri_rank + (uint32_t)q;
                 const float* p = pos + 9 * (size_t)tri;
                 tris_out[3 * (size_t)dst + 0] = make_float4(p[0], p[1], p[2], __uint_as_float(tri));
@@ -722,44 +872,85 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
         ds.bvh_depth = 0;
         if (n > 0) {
             const int T = 256;
-            const int nb = (n + T - 1) / T;
+            const int nbt = (n + T - 1) / T;
             float4* tlo = dev_alloc<float4>(n, temps);
             float4* thi = dev_alloc<float4>(n, temps);
             int* cb = dev_alloc<int>(6, temps);
             const int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
             BVH_CHECK(cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, stream));
-            k_tri_bounds<<<std::min(nb, 152 * 8), T, 0, stream>>>(d_pos, n, tlo, thi, cb);
-            uint64_t* keys = dev_alloc<uint64_t>(n, temps);
-            uint64_t* keys_s = dev_alloc<uint64_t>(n, temps);
-            uint32_t* vals = dev_alloc<uint32_t>(n, temps);
-            uint32_t* vals_s = dev_alloc<uint32_t>(n, temps);
-            k_morton<<<nb, T, 0, stream>>>(tlo, thi, n, cb, keys, vals);
-            size_t tmp_bytes = 0;
-            BVH_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_s, vals, vals_s, n, 0, 63, stream));
-            void* tmp = dev_alloc<uint8_t>(tmp_bytes, temps);
-            BVH_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_s, vals, vals_s, n, 0, 63, stream));
+            k_tri_bounds<<<std::min(nbt, 152 * 8), T, 0, stream>>>(d_pos, n, tlo, thi, cb);
 
-            const int ni = std::max(n - 1, 1);
+            // pre-splitting: m references (m = n when no triangle is split)
+            uint32_t* pieces = dev_alloc<uint32_t>(n, temps);
+            unsigned long long* extra_d = dev_alloc<unsigned long long>(1, temps);
+            BVH_CHECK(cudaMemsetAsync(extra_d, 0, sizeof(unsigned long long), stream));
+            k_split_counts<<<nbt, T, 0, stream>>>(d_pos, tlo, thi, n, pieces, extra_d);
+            BVH_CHECK(cudaGetLastError());
+            unsigned long long extra = 0;
+            BVH_CHECK(cudaMemcpyAsync(&extra, extra_d, sizeof(extra), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            const double budget = kSplitBudget * (double)n;
+            if ((double)extra > budget) {
+                k_split_scale<<<nbt, T, 0, stream>>>(pieces, n, budget / (double)extra);
+                BVH_CHECK(cudaGetLastError());
+            }
+            uint32_t* first = dev_alloc<uint32_t>((size_t)n + 1, temps);
+            size_t scan_bytes0 = 0;
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes0, pieces, first, n, stream));
+            void* scan_tmp0 = dev_alloc<uint8_t>(scan_bytes0, temps);
+            BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp0, scan_bytes0, pieces, first, n, stream));
+            uint32_t last_first = 0, last_pieces = 0;
+            BVH_CHECK(cudaMemcpyAsync(&last_first, first + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaMemcpyAsync(&last_pieces, pieces + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+            BVH_CHECK(cudaStreamSynchronize(stream));
+            const int64_t m64 = (int64_t)last_first + last_pieces;
+            if (m64 < n || m64 > (int64_t)n + (int64_t)budget + 1 || m64 > (int64_t)INT32_MAX / 2)
+                throw DeviceError("BVH pre-splitting produced " + std::to_string(m64) + " references for " +
+                                  std::to_string(n) + " triangles");
+            const int m = (int)m64;
+            float4* rlo = tlo;
+            float4* rhi = thi;
+            uint32_t* ref_tri = dev_alloc<uint32_t>(m, temps);
+            if (m > n) {
+                rlo = dev_alloc<float4>(m, temps);
+                rhi = dev_alloc<float4>(m, temps);
+                BVH_CHECK(cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+            }
+            k_split_emit<<<nbt, T, 0, stream>>>(d_pos, tlo, thi, n, pieces, first, rlo, rhi, ref_tri);
+            BVH_CHECK(cudaGetLastError());
+            const int nb = (m + T - 1) / T;
+            if (m > n) k_centroid_bounds<<<std::min(nb, 152 * 8), T, 0, stream>>>(rlo, rhi, m, cb);
+
+            uint64_t* keys = dev_alloc<uint64_t>(m, temps);
+            uint64_t* keys_s = dev_alloc<uint64_t>(m, temps);
+            uint32_t* vals = dev_alloc<uint32_t>(m, temps);
+            uint32_t* vals_s = dev_alloc<uint32_t>(m, temps);
+            k_morton<<<nb, T, 0, stream>>>(rlo, rhi, m, cb, keys, vals);
+            size_t tmp_bytes = 0;
+            BVH_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys_s, vals, vals_s, m, 0, 63, stream));
+            void* tmp = dev_alloc<uint8_t>(tmp_bytes, temps);
+            BVH_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_s, vals, vals_s, m, 0, 63, stream));
+            const int ni = std::max(m - 1, 1);
             uint32_t* left = dev_alloc<uint32_t>(ni, temps);
             uint32_t* right = dev_alloc<uint32_t>(ni, temps);
             int* int_parent = dev_alloc<int>(ni, temps);
-            int* leaf_parent = dev_alloc<int>(n, temps);
+            int* leaf_parent = dev_alloc<int>(m, temps);
             int2* range = dev_alloc<int2>(ni, temps);
-            float4* leaf_lo = dev_alloc<float4>(n, temps);
-            float4* leaf_hi = dev_alloc<float4>(n, temps);
+            float4* leaf_lo = dev_alloc<float4>(m, temps);
+            float4* leaf_hi = dev_alloc<float4>(m, temps);
             float4* int_lo = dev_alloc<float4>(ni, temps);
             float4* int_hi = dev_alloc<float4>(ni, temps);
             int* arrivals = dev_alloc<int>(ni + 1, temps);  // last entry: error flag
             BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));
-            uint32_t root_ref = n == 1 ? (kLeafFlag | 0u) : 0u;
-            uint32_t* leaf_tri = vals_s;  // triangle of each leaf position
-            if (n == 1) {
+            uint32_t root_ref = m == 1 ? (kLeafFlag | 0u) : 0u;
+            uint32_t* leaf_tri = vals_s;  // reference of each leaf position
+            if (m == 1) {
                 // a single leaf: its box is the triangle's
                 BVH_CHECK(cudaMemsetAsync(leaf_parent, 0xFF, sizeof(int), stream));  // -1
-                k_leaf_gather<<<1, 32, 0, stream>>>(1, vals_s, tlo, thi, leaf_lo, leaf_hi, left);
+                k_leaf_gather<<<1, 32, 0, stream>>>(1, vals_s, rlo, rhi, leaf_lo, leaf_hi, left);
                 BVH_CHECK(cudaGetLastError());
             } else {
-                root_ref = BuildPloc(n, vals_s, tlo, thi, left, right, int_parent, leaf_parent, range, leaf_lo, leaf_hi,
+                root_ref = BuildPloc(m, vals_s, rlo, rhi, left, right, int_parent, leaf_parent, range, leaf_lo, leaf_hi,
                                      int_lo, int_hi, arrivals, leaf_tri, temps, stream);
             }
 
@@ -769,8 +960,8 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             BVH_CHECK(cudaMalloc(&nodes, max_nodes * sizeof(CwNode)));
             temps.push_back(nodes);
             float4* tris_out = nullptr;
-            BVH_CHECK(cudaMalloc(&tris_out, 3 * (size_t)n * sizeof(float4)));
-            uint32_t* perm = dev_alloc<uint32_t>(n, temps);
+            BVH_CHECK(cudaMalloc(&tris_out, 3 * (size_t)m * sizeof(float4)));
+            uint32_t* perm = dev_alloc<uint32_t>(m, temps);
             WorkItem* work_a = dev_alloc<WorkItem>(max_nodes, temps);
             WorkItem* work_b = dev_alloc<WorkItem>(max_nodes, temps);
             uint32_t* children = dev_alloc<uint32_t>(8 * max_nodes, temps);
@@ -786,11 +977,11 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             BVH_CHECK(cudaMemcpyAsync(work_a, &root, sizeof(root), cudaMemcpyHostToDevice, stream));
             BinView bv{left, right, range, leaf_lo, leaf_hi, int_lo, int_hi};
             uint2* split = nullptr;
-            if (n > 1) {
+            if (m > 1) {
                 float4* cost = dev_alloc<float4>(2 * (size_t)ni, temps);
                 split = dev_alloc<uint2>(ni, temps);
                 BVH_CHECK(cudaMemsetAsync(arrivals, 0, sizeof(int) * (ni + 1), stream));
-                k_collapse_costs<<<nb, T, 0, stream>>>(n, bv, int_parent, leaf_parent, cost, split, arrivals,
+                k_collapse_costs<<<nb, T, 0, stream>>>(m, bv, int_parent, leaf_parent, cost, split, arrivals,
                                                        arrivals + ni);
                 BVH_CHECK(cudaGetLastError());
                 int dp_err = 0;
@@ -809,7 +1000,7 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_int, int_off, nwork + 1, stream));
                 BVH_CHECK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, n_tri, tri_off, nwork + 1, stream));
                 k_collapse_emit<<<gb, 128, 0, stream>>>(bv, work_a, nwork, children, int_off, tri_off, node_count,
-                                                       tri_count, leaf_tri, d_pos, nodes, tris_out, perm, work_b);
+                                                       tri_count, leaf_tri, ref_tri, d_pos, nodes, tris_out, perm, work_b);
                 BVH_CHECK(cudaGetLastError());
                 int totals[2];
                 BVH_CHECK(cudaMemcpyAsync(&totals[0], int_off + nwork, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -821,9 +1012,9 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
                 std::swap(work_a, work_b);
                 if (depth > 4096) throw DeviceError("BVH collapse did not terminate");
             }
-            if ((int)tri_count != n) {
+            if ((int)tri_count != m) {
                 cudaFree(tris_out);
-                throw DeviceError("BVH collapse lost triangles: " + std::to_string(tri_count) + " of " + std::to_string(n));
+                throw DeviceError("BVH collapse lost triangles: " + std::to_string(tri_count) + " of " + std::to_string(m));
             }
             // Shrink the node array to its exact size.
             CwNode* nodes_exact = nullptr;
@@ -831,10 +1022,11 @@ void BuildBvh(DeviceScene& ds, const float* d_pos, const float* d_nrm, const flo
             BVH_CHECK(cudaMemcpyAsync(nodes_exact, nodes, (size_t)node_count * sizeof(CwNode), cudaMemcpyDeviceToDevice, stream));
             float4* nrm_out = nullptr;
             float2* uv_out = nullptr;
-            BVH_CHECK(cudaMalloc(&nrm_out, 3 * (size_t)n * sizeof(float4)));
-            BVH_CHECK(cudaMalloc(&uv_out, 3 * (size_t)n * sizeof(float2)));
-            k_gather_shading<<<nb, T, 0, stream>>>(n, perm, d_nrm, d_uv, d_tri_prim, nrm_out, uv_out);
+            BVH_CHECK(cudaMalloc(&nrm_out, 3 * (size_t)m * sizeof(float4)));
+            BVH_CHECK(cudaMalloc(&uv_out, 3 * (size_t)m * sizeof(float2)));
+            k_gather_shading<<<nb, T, 0, stream>>>(m, perm, d_nrm, d_uv, d_tri_prim, nrm_out, uv_out);
             BVH_CHECK(cudaGetLastError());
+            ds.num_tris = m;
             ds.nodes = nodes_exact;
             ds.tris = tris_out;
             ds.nrm = nrm_out;
