@@ -301,9 +301,15 @@ def test_oracle_bdpt_matches_pt_with_area_lights(oracle_lib):
 
     o = OracleScene.from_desc(scenegen.material_box(with_point=False, with_directional=False), 1.0)
     W = H = 8
-    kw = dict(num_samples=W * H * 4096, max_vertices=8, width=W, height=H, rng_mode="reference")
-    pt = o.render("pt", seed=1, **kw)
-    pt2 = o.render("pt", seed=2, **kw)
-    b = o.render("bdpt", seed=3, **kw)
-    assert abs(b.sum() / pt.sum() - 1) < 0.03
+    K = 4
+    kw = dict(num_samples=W * H * 1024, max_vertices=8, width=W, height=H, rng_mode="reference")
+    pts = np.stack([o.render("pt", seed=1 + k, **kw) for k in range(K)])
+    bs = np.stack([o.render("bdpt", seed=101 + k, **kw) for k in range(K)])
+    # image sums: same expectation within 4 standard errors (independent renders give the noise)
+    sp, sb = pts.reshape(K, -1).sum(1), bs.reshape(K, -1).sum(1)
+    z = (sb.mean() - sp.mean()) / np.sqrt(sp.var(ddof=1) / K + sb.var(ddof=1) / K)
+    assert abs(z) < 4.0, (z, sb.mean() / sp.mean())
+    assert abs(sb.mean() / sp.mean() - 1) < 0.05
+    # per pixel: bdpt is no farther from pt than two pt renders are from each other (up to noise)
+    pt, pt2, b = pts[:2].mean(0), pts[2:].mean(0), bs[:2].mean(0)
     assert np.sqrt(((b - pt) ** 2).sum()) < 1.5 * np.sqrt(((pt2 - pt) ** 2).sum())
