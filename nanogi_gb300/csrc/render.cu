@@ -422,6 +422,29 @@ NGI_D void emit_shadow(const WaveView<R>& w, const ShadowRay<R>& sr, int job, co
     }
 }
 
+// The shading kernel stages its shadow rays in shared memory instead: one entry per thread and
+// item, claimed in the global shadow queue with the block's other claims (one atomic per block).
+template <typename R>
+struct alignas(16) StagedShadow {
+    float4 o, d;
+    Vec4T<R> c;
+    uint32_t pixel;
+};
+template <typename R>
+NGI_D StagedShadow<R>* shadow_stage() {
+    __shared__ StagedShadow<R> stage[kLogicBlock];
+    return stage;
+}
+template <typename R>
+NGI_D void stage_shadow(const ShadowRay<R>& sr, StagedShadow<R>* stage, int* count) {
+    if (!sr.valid) return;
+    const int i = atomicAdd(count, 1);  // shared memory: at most one ray per thread and item
+    stage[i].o = make_float4(sr.ox, sr.oy, sr.oz, sr.tmin);
+    stage[i].d = make_float4(sr.dx, sr.dy, sr.dz, sr.tmax);
+    stage[i].c = Vec4T<R>{sr.c.x, sr.c.y, sr.c.z, R(0)};
+    stage[i].pixel = sr.pixel;
+}
+
 // Next-event estimation at a vertex (src/nanogi.cpp:654-707).
 template <typename R>
 NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom<R>& g, bool at_sensor,
@@ -589,9 +612,12 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
     // against one atomic per warp: 1939 against 1805 Mrays/s, the logic kernels' time per iteration
     // 0.276 against 0.338 ms (regeneration alone: 1872 and 0.307 ms). The warps of a wave's logic
     // kernels all claim from the same few counters, and those returning atomics queue at one L2 slice.
-    __shared__ int s_warp[kLogicBlock / 32];
+    __shared__ int s_warp[kLogicBlock / 32], s_warp2[kLogicBlock / 32];
     __shared__ unsigned long long s_base64;
-    __shared__ int s_base32;
+    __shared__ int s_base32, s_base32b;
+    // shading: shadow rays staged in shared memory this item, and their claimed queue range
+    __shared__ int s_staged, s_staged_n, s_staged_base;
+    if (threadIdx.x == 0) s_staged = 0;  // the first barrier below comes before any staging
     const int stride = gridDim.x * blockDim.x;
     NGI_COUNTS_DECL
     block_counts_init(bc);
@@ -677,7 +703,8 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
                             const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
                             ShadowRay<R> sa;
                             next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
-                            emit_shadow<R, ADJ, BATCH>(w, sa, job, pa, pb, nv - 2, prim);
+                            if constexpr (PART == kLogicShadeQ && !ADJ) stage_shadow(sa, shadow_stage<R>(), &s_staged);
+                            else emit_shadow<R, ADJ, BATCH>(w, sa, job, pa, pb, nv - 2, prim);
                             dead = next_hit_is_dead(rc, un.w, nv);
                         }
                         const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
@@ -708,17 +735,50 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             if (!alive) need_new = true;
         }
 
-        if (PART == kLogicShadeQ) {
-            // ---- hand the slots whose path ended to the regeneration kernel ----
-            const int q = block_claim(&w.ctr->regen_count, need_new, s_warp, &s_base32);
-            if (need_new) w.regen_queue[q] = s;
+        if constexpr (PART == kLogicShadeQ) {
+            // ---- hand the slots whose path ended to the regeneration kernel, queue the continuing
+            // paths' rays and the staged shadow rays: one atomic per queue for the whole block ----
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
             if (valid) w.state[s] = st;
-            {
-                const int q2 = block_claim(w.ext_count, want_ext, s_warp, &s_base32);
-                if (want_ext) w.ext_queue[q2] = s;
+            const unsigned mr = __ballot_sync(0xFFFFFFFFu, need_new), me = __ballot_sync(0xFFFFFFFFu, want_ext);
+            const int warp = (int)(threadIdx.x >> 5);
+            if (lane_id() == 0) {
+                s_warp[warp] = __popc(mr);
+                s_warp2[warp] = __popc(me);
             }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int tr = 0, te = 0;
+                for (int k = 0; k < kLogicBlock / 32; k++) {
+                    const int cr = s_warp[k], ce = s_warp2[k];
+                    s_warp[k] = tr;
+                    s_warp2[k] = te;
+                    tr += cr;
+                    te += ce;
+                }
+                s_base32 = tr ? atomicAdd(&w.ctr->regen_count, tr) : 0;
+                s_base32b = te ? atomicAdd(w.ext_count, te) : 0;
+                if constexpr (!ADJ) {
+                    s_staged_n = s_staged;
+                    s_staged_base = s_staged ? atomicAdd(&w.ctr->sh_count, s_staged) : 0;
+                    s_staged = 0;  // every thread has staged this item's ray (it passed the barrier above)
+                }
+            }
+            __syncthreads();
+            if (need_new) w.regen_queue[s_base32 + s_warp[warp] + __popc(mr & lanemask_lt())] = s;
+            if (want_ext) w.ext_queue[s_base32b + s_warp2[warp] + __popc(me & lanemask_lt())] = s;
+            if constexpr (!ADJ) {
+                const StagedShadow<R>* stage = shadow_stage<R>();
+                for (int t = (int)threadIdx.x; t < s_staged_n; t += kLogicBlock) {
+                    const int q = s_staged_base + t;
+                    w.sh_o[q] = stage[t].o;
+                    w.sh_d[q] = stage[t].d;
+                    w.sh_c[q] = stage[t].c;
+                    w.sh_pix[q] = stage[t].pixel;
+                }
+            }
+            __syncthreads();  // the scratch and the stage are reused by the next item
             block_count_warp(&bc.active, st != SLOT_DONE && !need_new);  // the others: counted by regeneration
             continue;
         }
