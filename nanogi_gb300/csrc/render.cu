@@ -216,6 +216,34 @@ NGI_D T block_claim(T* counter, bool want, int* s_warp, T* s_base) {
     __syncthreads();  // the scratch is reused by the next claim
     return idx;
 }
+// Two block-wide claims in one step (three barriers instead of six): entries of c0 for the threads
+// with w0, of c1 for those with w1. c0 may be null (no claim; w0 must then be false).
+NGI_D void block_claim2(int* c0, bool w0, int* c1, bool w1, int& q0, int& q1, int* s_warp0, int* s_warp1,
+                        int* s_base) {
+    const unsigned m0 = __ballot_sync(0xFFFFFFFFu, w0), m1 = __ballot_sync(0xFFFFFFFFu, w1);
+    const int warp = (int)(threadIdx.x >> 5);
+    if (lane_id() == 0) {
+        s_warp0[warp] = __popc(m0);
+        s_warp1[warp] = __popc(m1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t0 = 0, t1 = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+            const int a = s_warp0[k], b = s_warp1[k];
+            s_warp0[k] = t0;
+            s_warp1[k] = t1;
+            t0 += a;
+            t1 += b;
+        }
+        s_base[0] = t0 ? atomicAdd(c0, t0) : 0;
+        s_base[1] = t1 ? atomicAdd(c1, t1) : 0;
+    }
+    __syncthreads();
+    q0 = s_base[0] + s_warp0[warp] + __popc(m0 & lanemask_lt());
+    q1 = s_base[1] + s_warp1[warp] + __popc(m1 & lanemask_lt());
+    __syncthreads();  // the scratch is reused by the next claim
+}
 // Adds per-thread counts (traversal statistics) into a global counter with one atomic per warp;
 // called where every lane of the warp is present.
 NGI_D void warp_sum_add(unsigned long long* counter, uint32_t v) {
@@ -614,7 +642,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
     // kernels all claim from the same few counters, and those returning atomics queue at one L2 slice.
     __shared__ int s_warp[kLogicBlock / 32], s_warp2[kLogicBlock / 32];
     __shared__ unsigned long long s_base64;
-    __shared__ int s_base32, s_base32b;
+    __shared__ int s_base32, s_base32b, s_base2[2];
     // shading: shadow rays staged in shared memory this item, and their claimed queue range
     __shared__ int s_staged, s_staged_n, s_staged_base;
     if (threadIdx.x == 0) s_staged = 0;  // the first barrier below comes before any staging
@@ -897,15 +925,13 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
         if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
         if (want_ext) st = SLOT_ACTIVE;
         if (valid) w.state[s] = st;
-        if (PART == kLogicRegen && w.carry_out) {
-            // compacted shading visits only queued slots: one left empty waits in the carry queue
-            const bool carry = valid && st == SLOT_EMPTY;
-            const int q = block_claim(w.carry_out_count, carry, s_warp, &s_base32);
-            if (carry) w.carry_out[q] = s;
-        }
         {
-            const int q = block_claim(w.ext_count, want_ext, s_warp, &s_base32);
-            if (want_ext) w.ext_queue[q] = s;
+            // compacted shading visits only queued slots: one left empty waits in the carry queue
+            const bool carry = PART == kLogicRegen && w.carry_out && valid && st == SLOT_EMPTY;
+            int qc, qe;
+            block_claim2(w.carry_out_count, carry, w.ext_count, want_ext, qc, qe, s_warp, s_warp2, s_base2);
+            if (carry) w.carry_out[qc] = s;
+            if (want_ext) w.ext_queue[qe] = s;
         }
         block_count_warp(&bc.active, valid && st != SLOT_DONE);
     }
