@@ -479,8 +479,10 @@ def main():
             totals["rays"] += st["extension_rays"] + st["shadow_rays"]
             totals["samples"] += st["camera_rays"]
             # ptdirect: counter reset, shading, regeneration and traversal per iteration, plus the
-            # wave's initial carry queue; pt: the fused path logic and traversal
+            # wave's initial carry queue; pt: the fused path logic and traversal; both: the wave-end
+            # launch that runs the last paths to their end
             totals["launches"] += (4 * st["iterations"] + 1) if RENDERER == "ptdirect" else 2 * st["iterations"]
+            totals["launches"] += 1 if st["finish_paths"] > 0 else 0
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)

@@ -127,6 +127,10 @@ typedef struct ngi_render_stats {
     int64_t logic_launches, extend_launches, shadow_launches;
     /* NGI_RENDER_TRAVERSAL_COUNTERS: nodes / triangles visited, over all rays of each kind */
     int64_t extend_nodes, extend_tris, shadow_nodes, shadow_tris;
+    /* pt / ptdirect camera paths: once every sample is claimed and few paths remain, one launch
+     * runs each remaining path to its end (one thread per path). The paths it ran; 0 when the wave
+     * drained without it. */
+    int64_t finish_paths;
 } ngi_render_stats;
 
 /* Scene summary (host side; available without a GPU). */

@@ -73,6 +73,7 @@ class RenderStats(ctypes.Structure):
         ("extend_tris", ctypes.c_int64),
         ("shadow_nodes", ctypes.c_int64),
         ("shadow_tris", ctypes.c_int64),
+        ("finish_paths", ctypes.c_int64),
     ]
 
 

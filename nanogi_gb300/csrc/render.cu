@@ -67,7 +67,7 @@ struct WaveCounters {
     int ext_fetch;                    // rays handed out by the persistent traversal kernel
     int sh_fetch;                     // rays handed out by the shadow-only traversal kernel
     int regen_count;                  // slots handed from path shading to regeneration
-    int error_flags;                  // bit 0: traversal stack overflow
+    int error_flags;                  // bit 0: traversal stack overflow, 1: adjoint prefix, 2: wave-end vertex cap
     int ext_count_b;                  // compacted shading: count of the second extension queue
     int carry_count[2];               //   and of the two carry queues (reset per iteration by parity)
     unsigned long long stat_camera;
@@ -453,7 +453,7 @@ NGI_D void emit_shadow(const WaveView<R>& w, const ShadowRay<R>& sr, int job, co
 // The shading kernel stages its shadow rays in shared memory instead: one entry per thread and
 // item, claimed in the global shadow queue with the block's other claims (one atomic per block).
 template <typename R>
-struct alignas(16) StagedShadow {
+struct StagedShadow {  // float4 members: 16-byte aligned (32 with a double colour)
     float4 o, d;
     Vec4T<R> c;
     uint32_t pixel;
@@ -606,6 +606,82 @@ NGI_D bool next_hit_is_dead(const RenderConsts& rc, float next_rr, int nv) {
     return next_rr > 0.5f || (rc.max_vertices != -1 && nv + 1 >= rc.max_vertices);
 }
 
+// One path vertex of pt / ptdirect at the hit h of slot s's extension ray (src/nanogi.cpp:557-603
+// and 646-799): emission on a light hit (pt), Russian roulette, next-event estimation (ptdirect; its
+// shadow ray goes to emit(ray, prefix length, vertex primitive) at once, so that it holds no registers
+// during the BSDF sampling), the BSDF sample, and the continuation ray stored in the slot. Returns true
+// when the path continues. The adjoint's surface-vertex prefix is pa / pb.
+template <typename R, bool ADJ, typename Emit>
+NGI_D bool shade_vertex(const SceneView<R>& sv, const RenderConsts& rc, double* film, bool direct,
+                        const WaveView<R>& w, int s, float4 h, uint4& pa, uint4& pb, float* gsm, BlockCounts& bc,
+                        Emit&& emit) {
+    V3<R> d;
+    Geom<R> g;
+    const int prim = hit_geometry(sv, rc, w, s, h, d, g, false);
+    const Vec4T<R> t4 = w.thr[s];
+    V3<R> thr = v3<R>(t4.x, t4.y, t4.z);
+    const uint32_t pixel = w.pixel[s];
+    const unsigned long long sample = w.sample[s];
+    int nv = w.nverts[s];
+    const RngKey rk = make_rng(rc.seed, sample);
+
+    const DevMaterial<R>& mat = sv.mats[prim];
+    if (ADJ) {
+        pa = w.pre[2 * (size_t)s];
+        pb = w.pre[2 * (size_t)s + 1];
+    }
+
+    if (!direct && (mat.type & DT_L) && mat.l_type == LT_AREA) {
+        // Emission on a light hit (src/nanogi.cpp:568-575)
+        if (dot(g.sn, -d) > R(0)) {
+            const V3<R> c = thr * mat.Le;
+            if (!is_zero(c)) {
+                if (finite3(c)) {
+                    film_add(film, pixel, c);
+                    atomicAdd(&bc.contrib, 1u);
+                    if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim, gsm, rc.num_prims);
+                } else {
+                    atomicAdd(&bc.nonfinite, 1u);
+                }
+            }
+        }
+    }
+    // Russian roulette after every hit (src/nanogi.cpp:583-591)
+    const float rr = rng4(rk, (uint32_t)nv, RNG_NEE_RR).w;
+    if (rr > 0.5f) return false;
+    thr = thr / R(0.5);
+    nv++;
+    if ((rc.max_vertices != -1 && nv >= rc.max_vertices) || mat.bsdf == BSDF_NONE) return false;
+    tangent_space(g);
+    const V3<R> wi = -d;
+    bool dead = false;
+    if (direct) {
+        const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
+        ShadowRay<R> sa;
+        next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
+        emit(sa, nv - 2, prim);
+        dead = next_hit_is_dead(rc, un.w, nv);
+    }
+    const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
+    V3<R> wo, wgt;
+    if (dead || !bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y, (R)ud.z, wo, wgt))
+        return false;
+    thr = thr * wgt;
+    if (ADJ) {
+        if (nv - 2 >= kAdjMaxPrefix) {
+            atomicOr(&w.ctr->error_flags, 2);
+        } else {
+            prefix_set(pa, pb, nv - 2, (uint32_t)prim);
+            w.pre[2 * (size_t)s] = pa;
+            w.pre[2 * (size_t)s + 1] = pb;
+        }
+    }
+    store_ray(w, s, g, wo, rc.ray_offset);
+    w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+    w.nverts[s] = nv;
+    return true;
+}
+
 // PART: kLogicFused does both halves of an iteration in one kernel; kLogicShadeQ consumes the
 // hits, does next-event estimation and continues the paths, handing the slots whose path ended to
 // kLogicRegen, which starts new samples in them (two kernels of half the code each: the fused
@@ -680,85 +756,20 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
             bool alive = false;
             const float4 h = w.hit[s];
-            const int ti = __float_as_int(h.w);
-            if (ti >= 0) {
+            if (__float_as_int(h.w) >= 0) {
                 const int job = BATCH ? w.job[s] : 0;
                 const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
                 const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
                 double* const film = BATCH ? jobs[job].film : w.film;
                 const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
-                V3<R> d;
-                Geom<R> g;
-                const int prim = hit_geometry(sv, rc, w, s, h, d, g, false);
-                const Vec4T<R> t4 = w.thr[s];
-                V3<R> thr = v3<R>(t4.x, t4.y, t4.z);
-                const uint32_t pixel = w.pixel[s];
-                const unsigned long long sample = w.sample[s];
-                int nv = w.nverts[s];
-                const RngKey rk = make_rng(rc.seed, sample);
-
-                const DevMaterial<R>& mat = sv.mats[prim];
-                if (ADJ) {
-                    pa = w.pre[2 * (size_t)s];
-                    pb = w.pre[2 * (size_t)s + 1];
-                }
-
-                if (!direct && (mat.type & DT_L) && mat.l_type == LT_AREA) {
-                    // Emission on a light hit (src/nanogi.cpp:568-575)
-                    if (dot(g.sn, -d) > R(0)) {
-                        const V3<R> c = thr * mat.Le;
-                        if (!is_zero(c)) {
-                            if (finite3(c)) {
-                                film_add(film, pixel, c);
-                                atomicAdd(&bc.contrib, 1u);
-                                if (ADJ) adj_accumulate(w, sv, pixel, c, pa, pb, nv - 1, -1, prim, gsm, rc.num_prims);
-                            } else {
-                                atomicAdd(&bc.nonfinite, 1u);
-                            }
-                        }
-                    }
-                }
-                // Russian roulette after every hit (src/nanogi.cpp:583-591)
-                const float rr = rng4(rk, (uint32_t)nv, RNG_NEE_RR).w;
-                if (!(rr > 0.5f)) {
-                    thr = thr / R(0.5);
-                    nv++;
-                    if (!(rc.max_vertices != -1 && nv >= rc.max_vertices) && mat.bsdf != BSDF_NONE) {
-                        tangent_space(g);
-                        const V3<R> wi = -d;
-                        bool dead = false;
-                        if (direct) {
-                            const float4 un = rng4(rk, (uint32_t)nv, RNG_NEE_RR);
-                            ShadowRay<R> sa;
-                            next_event(sv, rc, g, false, &mat, wi, thr, pixel, un, sa);
-                            if constexpr (PART == kLogicShadeQ && !ADJ) stage_shadow(sa, shadow_stage<R>(), &s_staged);
-                            else emit_shadow<R, ADJ, BATCH>(w, sa, job, pa, pb, nv - 2, prim);
-                            dead = next_hit_is_dead(rc, un.w, nv);
-                        }
-                        const float4 ud = rng4(rk, (uint32_t)nv, RNG_DIR);
-                        V3<R> wo, wgt;
-                        if (!dead && bsdf_sample_weight(mat, material_albedo(sv, mat, g), g, wi, (R)ud.x, (R)ud.y, (R)ud.z,
-                                               wo, wgt)) {
-                            {
-                                thr = thr * wgt;
-                                if (ADJ) {
-                                    if (nv - 2 >= kAdjMaxPrefix) {
-                                        atomicOr(&w.ctr->error_flags, 2);
-                                    } else {
-                                        prefix_set(pa, pb, nv - 2, (uint32_t)prim);
-                                        w.pre[2 * (size_t)s] = pa;
-                                        w.pre[2 * (size_t)s + 1] = pb;
-                                    }
-                                }
-                                store_ray(w, s, g, wo, rc.ray_offset);
-                                w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
-                                w.nverts[s] = nv;
-                                alive = true;
-                                want_ext = true;
-                            }
-                        }
-                    }
-                }
+                alive = shade_vertex<R, ADJ>(sv, rc, film, direct, w, s, h, pa, pb, gsm, bc,
+                                             [&](const ShadowRay<R>& sa, int count, int vprim) {
+                                                 if constexpr (PART == kLogicShadeQ && !ADJ)
+                                                     stage_shadow(sa, shadow_stage<R>(), &s_staged);
+                                                 else
+                                                     emit_shadow<R, ADJ, BATCH>(w, sa, job, pa, pb, count, vprim);
+                                             });
+                want_ext = alive;
             }
             if (!alive) need_new = true;
         }
@@ -808,132 +819,133 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             }
             __syncthreads();  // the scratch and the stage are reused by the next item
             block_count_warp(&bc.active, st != SLOT_DONE && !need_new);  // the others: counted by regeneration
-            continue;
-        }
-
-        // ---- claim a new sample for finished slots (path regeneration) ----
-        // A claimed sample whose camera ray is not traced (its first hit is dead, or the ray leaves
-        // the raster) leaves the slot empty; the slot then claims the next sample, up to
-        // kRegenAttempts samples per iteration (each may add its sensor connection to the shadow
-        // queue). Terrain, ptdirect: 1 attempt 1776, 2 attempts 1833, 3 attempts 1824 Msamples/s.
-        for (int attempt = 0; attempt < kRegenAttempts; attempt++) {
-            {
-                // one atomic per block on the sample counter every slot of the wave claims from
-                const unsigned long long k = block_claim(&w.ctr->next_sample, need_new, s_warp, &s_base64);
-                if (need_new) {
-                    int job = 0;
-                    unsigned long long local = k;
-                    if (BATCH && k < (unsigned long long)rc0.num_samples) {
-                        // job of batch sample k: last job whose first sample is <= k
-                        int lo = 0, hi = num_jobs - 1;
-                        while (lo < hi) {
-                            const int mid = (lo + hi + 1) >> 1;
-                            if ((unsigned long long)jobs[mid].sample_base <= k) lo = mid; else hi = mid - 1;
-                        }
-                        job = lo;
-                        local = k - (unsigned long long)jobs[job].sample_base;
-                    }
-                    const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
-                    const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
-                    const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
-                    if (k >= (unsigned long long)rc0.num_samples) {
-                        st = SLOT_DONE;
-                    } else if (rc.max_vertices == 1) {
-                        // the loop's first test ends the path before the sensor vertex does anything
-                        // (src/nanogi.cpp:485, 647): the sample counts, nothing is traced
-                        st = SLOT_EMPTY;
-                    } else {
-                        // ---- sensor vertex (src/nanogi.cpp:450-479, 609-641) ----
-                        const unsigned long long gsample = (unsigned long long)rc.sample_offset + local;
-                        const RngKey rk = make_rng(rc.seed, gsample);
-                        Geom<R> ge;
-                        V3<R> thr;
-                        const DevSensor<R>& cam = sv.sensor;
-                        bool ok = true;
-                        if (cam.type == ET_PINHOLE) {
-                            ge.p = cam.eye;
-                            ge.degenerated = true;
-                            ge.ext = 0.0f;
-                            ge.sn = ge.gn = ge.du = ge.dv = v3<R>(0, 0, 0);
-                            ge.uvx = ge.uvy = R(0);
-                            thr = v3<R>(1, 1, 1);
-                        } else {
-                            const float4 us = rng4(rk, 1u, RNG_SENSOR);
-                            sample_mesh_position(sv, cam.tri_base, cam.tri_count, cam.cdf_offset, (R)us.x, (R)us.y, ge);
-                            const R a = R(1) / cam.inv_area;
-                            thr = v3<R>(a, a, a);
-                        }
-                        if (direct) {
-                            const float4 un = rng4(rk, 1u, RNG_NEE_RR);
-                            ShadowRay<R> sb;
-                            next_event(sv, rc, ge, true, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, 0u, un, sb);
-                            // sensor vertex: no surface factors for the adjoint
-                            emit_shadow<R, ADJ, BATCH>(w, sb, job, pa, pb, 0, -1);
-                            if (next_hit_is_dead(rc, un.w, 1)) ok = false;  // the sample ends at the sensor vertex
-                        }
-                        const float4 ud = rng4(rk, 1u, RNG_DIR);
-                        V3<R> wo;
-                        uint32_t pix = 0;
-                        if (cam.type == ET_PINHOLE) {
-                            R rx, ry;
-                            if (rc.stratified && (long long)gsample < rc.strat_end) {
-                                const long long wh = (long long)rc.width * rc.height;
-                                const long long pidx = (long long)(gsample % (unsigned long long)wh);
-                                const int px = (int)(pidx % rc.width), py = (int)(pidx / rc.width);
-                                rx = ((R)px + (R)ud.x) / (R)rc.width;
-                                ry = ((R)py + (R)ud.y) / (R)rc.height;
-                            } else {
-                                rx = (R)ud.x;
-                                ry = (R)ud.y;
+        } else {
+            // ---- claim a new sample for finished slots (path regeneration) ----
+            // A claimed sample whose camera ray is not traced (its first hit is dead, or the ray leaves
+            // the raster) leaves the slot empty; the slot then claims the next sample, up to
+            // kRegenAttempts samples per iteration (each may add its sensor connection to the shadow
+            // queue). Terrain, ptdirect: 1 attempt 1776, 2 attempts 1833, 3 attempts 1824 Msamples/s.
+            for (int attempt = 0; attempt < kRegenAttempts; attempt++) {
+                {
+                    // one atomic per block on the sample counter every slot of the wave claims from
+                    const unsigned long long k = block_claim(&w.ctr->next_sample, need_new, s_warp, &s_base64);
+                    if (need_new) {
+                        int job = 0;
+                        unsigned long long local = k;
+                        if (BATCH && k < (unsigned long long)rc0.num_samples) {
+                            // job of batch sample k: last job whose first sample is <= k
+                            int lo = 0, hi = num_jobs - 1;
+                            while (lo < hi) {
+                                const int mid = (lo + hi + 1) >> 1;
+                                if ((unsigned long long)jobs[mid].sample_base <= k) lo = mid; else hi = mid - 1;
                             }
-                            wo = pinhole_direction(cam, rx, ry);
-                            R qx, qy;
-                            if (!pinhole_raster(cam, wo, qx, qy)) ok = false;
-                            else {
-                                pix = (uint32_t)pixel_index(qx, qy, rc.width, rc.height);
-                                const R W = pinhole_importance(cam, wo);
-                                if (W == R(0)) ok = false;
-                                else thr = thr * (W / W);
-                            }
-                        } else {
-                            const V3<R> l = cosine_hemisphere((R)ud.x, (R)ud.y);
-                            wo = to_world(ge, l);
-                            pix = (uint32_t)pixel_index(ge.uvx, ge.uvy, rc.width, rc.height);
-                            const V3<R> lw = to_local(ge, wo);
-                            if (!(lw.z > R(0)) || is_zero(cam.We)) ok = false;
-                            else thr = thr * cam.We / kInvPi_<R>();
+                            job = lo;
+                            local = k - (unsigned long long)jobs[job].sample_base;
                         }
-                        if (ok) {
-                            store_ray(w, s, ge, wo, rc.ray_offset);
-                            w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
-                            w.pixel[s] = pix;
-                            w.sample[s] = gsample;
-                            if (BATCH) w.job[s] = job;
-                            w.nverts[s] = 1;
-                            want_ext = true;
-                            st = SLOT_ACTIVE;
-                        } else {
+                        const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
+                        const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
+                        const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
+                        if (k >= (unsigned long long)rc0.num_samples) {
+                            st = SLOT_DONE;
+                        } else if (rc.max_vertices == 1) {
+                            // the loop's first test ends the path before the sensor vertex does anything
+                            // (src/nanogi.cpp:485, 647): the sample counts, nothing is traced
                             st = SLOT_EMPTY;
+                        } else {
+                            // ---- sensor vertex (src/nanogi.cpp:450-479, 609-641) ----
+                            const unsigned long long gsample = (unsigned long long)rc.sample_offset + local;
+                            const RngKey rk = make_rng(rc.seed, gsample);
+                            Geom<R> ge;
+                            V3<R> thr;
+                            const DevSensor<R>& cam = sv.sensor;
+                            bool ok = true;
+                            if (cam.type == ET_PINHOLE) {
+                                ge.p = cam.eye;
+                                ge.degenerated = true;
+                                ge.ext = 0.0f;
+                                ge.sn = ge.gn = ge.du = ge.dv = v3<R>(0, 0, 0);
+                                ge.uvx = ge.uvy = R(0);
+                                thr = v3<R>(1, 1, 1);
+                            } else {
+                                const float4 us = rng4(rk, 1u, RNG_SENSOR);
+                                sample_mesh_position(sv, cam.tri_base, cam.tri_count, cam.cdf_offset, (R)us.x, (R)us.y,
+                                                     ge);
+                                const R a = R(1) / cam.inv_area;
+                                thr = v3<R>(a, a, a);
+                            }
+                            if (direct) {
+                                const float4 un = rng4(rk, 1u, RNG_NEE_RR);
+                                ShadowRay<R> sb;
+                                next_event(sv, rc, ge, true, (const DevMaterial<R>*)nullptr, v3<R>(0, 0, 0), thr, 0u,
+                                           un, sb);
+                                // sensor vertex: no surface factors for the adjoint
+                                emit_shadow<R, ADJ, BATCH>(w, sb, job, pa, pb, 0, -1);
+                                if (next_hit_is_dead(rc, un.w, 1)) ok = false;  // the sample ends at the sensor vertex
+                            }
+                            const float4 ud = rng4(rk, 1u, RNG_DIR);
+                            V3<R> wo;
+                            uint32_t pix = 0;
+                            if (cam.type == ET_PINHOLE) {
+                                R rx, ry;
+                                if (rc.stratified && (long long)gsample < rc.strat_end) {
+                                    const long long wh = (long long)rc.width * rc.height;
+                                    const long long pidx = (long long)(gsample % (unsigned long long)wh);
+                                    const int px = (int)(pidx % rc.width), py = (int)(pidx / rc.width);
+                                    rx = ((R)px + (R)ud.x) / (R)rc.width;
+                                    ry = ((R)py + (R)ud.y) / (R)rc.height;
+                                } else {
+                                    rx = (R)ud.x;
+                                    ry = (R)ud.y;
+                                }
+                                wo = pinhole_direction(cam, rx, ry);
+                                R qx, qy;
+                                if (!pinhole_raster(cam, wo, qx, qy)) ok = false;
+                                else {
+                                    pix = (uint32_t)pixel_index(qx, qy, rc.width, rc.height);
+                                    const R W = pinhole_importance(cam, wo);
+                                    if (W == R(0)) ok = false;
+                                    else thr = thr * (W / W);
+                                }
+                            } else {
+                                const V3<R> l = cosine_hemisphere((R)ud.x, (R)ud.y);
+                                wo = to_world(ge, l);
+                                pix = (uint32_t)pixel_index(ge.uvx, ge.uvy, rc.width, rc.height);
+                                const V3<R> lw = to_local(ge, wo);
+                                if (!(lw.z > R(0)) || is_zero(cam.We)) ok = false;
+                                else thr = thr * cam.We / kInvPi_<R>();
+                            }
+                            if (ok) {
+                                store_ray(w, s, ge, wo, rc.ray_offset);
+                                w.thr[s] = Vec4T<R>{thr.x, thr.y, thr.z, R(0)};
+                                w.pixel[s] = pix;
+                                w.sample[s] = gsample;
+                                if (BATCH) w.job[s] = job;
+                                w.nverts[s] = 1;
+                                want_ext = true;
+                                st = SLOT_ACTIVE;
+                            } else {
+                                st = SLOT_EMPTY;
+                            }
                         }
                     }
+                    block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
                 }
-                block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
+                need_new = need_new && st == SLOT_EMPTY;
+                if (!__syncthreads_or(need_new)) break;  // block-uniform: the claims are block-wide
             }
-            need_new = need_new && st == SLOT_EMPTY;
-            if (!__syncthreads_or(need_new)) break;  // block-uniform: the claims are block-wide
+            if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
+            if (want_ext) st = SLOT_ACTIVE;
+            if (valid) w.state[s] = st;
+            {
+                // compacted shading visits only queued slots: one left empty waits in the carry queue
+                const bool carry = PART == kLogicRegen && w.carry_out && valid && st == SLOT_EMPTY;
+                int qc, qe;
+                block_claim2(w.carry_out_count, carry, w.ext_count, want_ext, qc, qe, s_warp, s_warp2, s_base2);
+                if (carry) w.carry_out[qc] = s;
+                if (want_ext) w.ext_queue[qe] = s;
+            }
+            block_count_warp(&bc.active, valid && st != SLOT_DONE);
         }
-        if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
-        if (want_ext) st = SLOT_ACTIVE;
-        if (valid) w.state[s] = st;
-        {
-            // compacted shading visits only queued slots: one left empty waits in the carry queue
-            const bool carry = PART == kLogicRegen && w.carry_out && valid && st == SLOT_EMPTY;
-            int qc, qe;
-            block_claim2(w.carry_out_count, carry, w.ext_count, want_ext, qc, qe, s_warp, s_warp2, s_base2);
-            if (carry) w.carry_out[qc] = s;
-            if (want_ext) w.ext_queue[qe] = s;
-        }
-        block_count_warp(&bc.active, valid && st != SLOT_DONE);
     }
     block_counts_flush(bc, w.ctr);  // every thread of the block ran the same iterations
     if (ADJ && !DIRECT) adj_flush(w, gsm, rc0.num_prims);
@@ -1524,6 +1536,70 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
     }
 }
 
+// ---- the end of a wave ----------------------------------------------------------------------------
+// Once every sample has been claimed, the paths still in flight only get fewer with each iteration,
+// and the wave's last iterations run a handful of rays each at the price of a full set of launches.
+// k_finish takes over then: one thread per pending path runs it to its end, vertex after vertex, with
+// the shading of the wavefront kernels (shade_vertex) and the traversal inline (trace_ray: the closest
+// hit of each extension ray and the any-hit test of each shadow ray, which adds an unoccluded
+// contribution to the film). Every path follows the same Philox draws and traversal as in the
+// wavefront, so the film is the same up to the order of its FP64 sums.
+constexpr int kFinishBlock = 128;
+constexpr int kFinishMaxVertices = 4096;
+template <typename R, bool DIRECT>
+__global__ void __launch_bounds__(kFinishBlock) k_finish(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+    NGI_COUNTS_DECL
+    block_counts_init(bc);
+    __shared__ unsigned long long blk_ext, blk_sh;
+    if (threadIdx.x == 0) blk_ext = blk_sh = 0ull;
+    __syncthreads();
+    bool overflow = false;
+    uint32_t n_ext = 0, n_sh = 0;
+    const int n = min(*w.ext_count, w.Q);
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
+        const int s = w.ext_queue[item];
+        float4 h = w.hit[s];
+        uint4 pa = make_uint4(0u, 0u, 0u, 0u), pb = pa;
+        // a path ends by Russian roulette with probability 1/2 per vertex; the cap only bounds the loop
+        for (int vertex = 0; __float_as_int(h.w) >= 0; vertex++) {
+            if (vertex == kFinishMaxVertices) {
+                atomicOr(&w.ctr->error_flags, 4);
+                break;
+            }
+            const bool alive = shade_vertex<R, false>(
+                sv, rc, w.film, DIRECT, w, s, h, pa, pb, nullptr, bc, [&](const ShadowRay<R>& sa, int, int) {
+                    if (!sa.valid) return;
+                    float tmax = sa.tmax, u = 0.0f, v = 0.0f;
+                    const int occ = trace_ray<true, false>(sv.nodes, sv.tris, sv.num_nodes, sa.ox, sa.oy, sa.oz, sa.dx,
+                                                           sa.dy, sa.dz, sa.tmin, tmax, u, v, overflow, nullptr);
+                    n_sh++;
+                    if (occ >= 0) return;
+                    if (finite3(sa.c)) {
+                        film_add(w.film, sa.pixel, sa.c);
+                        atomicAdd(&bc.contrib, 1u);
+                    } else {
+                        atomicAdd(&bc.nonfinite, 1u);
+                    }
+                });
+            if (!alive) break;
+            const float4 o = w.ray_o[s], d = w.ray_d[s];
+            float tmax = d.w, u = 0.0f, v = 0.0f;
+            const int ti = trace_ray<false, false>(sv.nodes, sv.tris, sv.num_nodes, o.x, o.y, o.z, d.x, d.y, d.z, o.w,
+                                                   tmax, u, v, overflow, nullptr);
+            n_ext++;
+            h = make_float4(ti >= 0 ? tmax : d.w, u, v, __int_as_float(ti));
+        }
+    }
+    if (n_ext) atomicAdd(&blk_ext, (unsigned long long)n_ext);
+    if (n_sh) atomicAdd(&blk_sh, (unsigned long long)n_sh);
+    if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    block_counts_flush(bc, w.ctr);  // synchronises the block first
+    if (threadIdx.x == 0) {
+        if (blk_ext) atomicAdd(&w.ctr->stat_ext, blk_ext);
+        if (blk_sh) atomicAdd(&w.ctr->stat_shadow, blk_sh);
+    }
+}
+
 // ---- parity hooks --------------------------------------------------------------------------
 __global__ void k_intersect(const CwNode* nodes, const float4* tris, int num_nodes, const float4* rays, int64_t n,
                             int32_t* prim, float* t_out, float* uv_out, int* err) {
@@ -2008,6 +2084,11 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     }
     cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
     double kms[2] = {0, 0};
+    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, outside batches, the
+    // adjoint and the measurement renders (which time or count the wavefront kernels themselves)
+    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !BATCH && !STATS;
+    const int finish_max = std::max(v.Q / 32, 4096);
+    long long finish_paths = 0;
     long long launches = 0;
 
     long long iterations = 0;
@@ -2046,6 +2127,26 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
             if (wv->h_ctr->error_flags & 2)
                 throw DeviceError("adjoint path longer than 16 surface vertices", NGI_ERR_UNSUPPORTED);
             if (wv->h_ctr->active == 0 && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples) break;
+            if constexpr (finish) {
+                // every sample claimed and few paths left: run them to their end in one launch
+                const int pending = wv->h_ctr->ext_count;
+                if (!kernel_timing && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples &&
+                    pending <= finish_max) {
+                    if (pending > 0) {
+                        k_finish<R, DIRECT><<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, 0, stream>>>(
+                            sv, v, rc);
+                        CUDA_CHECK(cudaGetLastError());
+                        CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
+                                                   stream));
+                        CUDA_CHECK(cudaStreamSynchronize(stream));
+                        if (wv->h_ctr->error_flags & 1) throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+                        if (wv->h_ctr->error_flags & 4)
+                            throw DeviceError("a path outran the wave-end vertex cap", NGI_ERR_DEVICE_TIMEOUT);
+                        finish_paths = pending;
+                    }
+                    break;
+                }
+            }
             if (iterations > max_iters) throw DeviceError("wave did not drain", NGI_ERR_DEVICE_TIMEOUT);
         }
         CUDA_CHECK(cudaEventRecord(wv->ev1, stream));
@@ -2080,6 +2181,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     ds.last_stats.nonfinite = (int64_t)c.stat_nonfinite;
     ds.last_stats.iterations = iterations;
     ds.last_stats.render_ms = ms;
+    ds.last_stats.finish_paths = finish_paths;
 }
 
 }  // namespace

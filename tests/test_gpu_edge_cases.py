@@ -224,6 +224,7 @@ def test_scaled_ray_offsets_replay_the_oracle(native_lib, tmp_path, scale):
 def test_instrumented_renders_count_the_same_paths(native_lib, cornell, renderer):
     """Kernel timing and traversal counters change how a render is launched and observed, never
     what it computes: the film and every path count match the plain render of the same samples.
+    The plain render also hands its last paths to the wave-end kernel, the others do not.
     The counts themselves are summed per block in shared memory, so they are checked against what
     the sample count implies."""
     from nanogi_gb300 import capi
@@ -252,6 +253,11 @@ def test_instrumented_renders_count_the_same_paths(native_lib, cornell, renderer
         # (iterations differ: graph launches run whole groups of iterations, timed runs stop at the last)
         for k in ("camera_rays", "extension_rays", "shadow_rays", "film_contributions"):
             assert st[k] == st0[k], (flags, k)
+    # the plain render ends with the wave-end launch (one thread per remaining path); the timed
+    # one drains through the wavefront kernels alone, and both films are equal
+    assert 0 < st0["finish_paths"] <= 4096
+    assert runs[capi.KERNEL_TIMING][1]["finish_paths"] == 0
+    assert runs[capi.TRAVERSAL_COUNTERS][1]["finish_paths"] == 0
     st_t = runs[capi.KERNEL_TIMING][1]
     assert st_t["logic_launches"] == st_t["extend_launches"] == st_t["iterations"]
     assert st_t["shadow_launches"] == 0  # one traversal launch traces both queues
