@@ -333,14 +333,34 @@ NGI_D int cdf_sample_reuse(const double* __restrict__ cdf, int n, double u, doub
     return i;
 }
 
+// The same sample for the FP32 path, on the same FP64 cdf with a fraction of the FP64 arithmetic
+// (this GPU issues FP64 at 1/64 of the FP32 rate). The cdf entries and u are non-negative, and
+// non-negative IEEE-754 doubles order like their bit patterns read as integers: the search compares
+// those, so it returns the index the FP64 comparisons give. The reused variable takes the two
+// differences in FP64 and their quotient in FP32 (within an FP32 ulp or so of the FP64 quotient).
+NGI_D int cdf_sample_reuse(const double* __restrict__ cdf, int n, float u, float& u2) {
+    const double ud = (double)u;
+    const long long ub = __double_as_longlong(ud);
+    int lo = 0, hi = n + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__double_as_longlong(cdf[mid]) > ub) hi = mid; else lo = mid + 1;
+    }
+    int i = lo - 1;
+    i = i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+    const double c0 = cdf[i];
+    u2 = (float)(ud - c0) / (float)(cdf[i + 1] - c0);
+    return i;
+}
+
 // SamplePosition on a triangle mesh emitter (rt.hpp:488-526).
 template <typename R>
 NGI_D void sample_mesh_position(const SceneView<R>& sv, int tri_base, int tri_count, int cdf_offset, R u0, R u1,
                                 Geom<R>& g) {
-    double u2d;
-    const int i = cdf_sample_reuse(sv.cdf + cdf_offset, tri_count, (double)u0, u2d);
+    R u2;
+    const int i = cdf_sample_reuse(sv.cdf + cdf_offset, tri_count, u0, u2);
     R b0, b1;
-    uniform_triangle((R)u2d, u1, b0, b1);
+    uniform_triangle(u2, u1, b0, b1);
     const float* P = sv.emit_tri_pos + 9 * (size_t)(tri_base + i);
     const V3<R> p1 = v3<R>(P[0], P[1], P[2]), p2 = v3<R>(P[3], P[4], P[5]), p3 = v3<R>(P[6], P[7], P[8]);
     g.p = p1 * (R(1) - b0 - b1) + p2 * b0 + p3 * b1;

@@ -888,9 +888,14 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
                             if (cam.type == ET_PINHOLE) {
                                 R rx, ry;
                                 if (rc.stratified && (long long)gsample < rc.strat_end) {
-                                    const long long wh = (long long)rc.width * rc.height;
-                                    const long long pidx = (long long)(gsample % (unsigned long long)wh);
-                                    const int px = (int)(pidx % rc.width), py = (int)(pidx / rc.width);
+                                    // 32-bit division where the sample index fits (a film has fewer
+                                    // than 2^31 pixels); 64-bit division is far slower on the GPU
+                                    const uint32_t wh = (uint32_t)rc.width * (uint32_t)rc.height;
+                                    const uint32_t pidx = (gsample >> 32) == 0ull
+                                                              ? (uint32_t)gsample % wh
+                                                              : (uint32_t)(gsample % (unsigned long long)wh);
+                                    const int px = (int)(pidx % (uint32_t)rc.width);
+                                    const int py = (int)(pidx / (uint32_t)rc.width);
                                     rx = ((R)px + (R)ud.x) / (R)rc.width;
                                     ry = ((R)py + (R)ud.y) / (R)rc.height;
                                 } else {
@@ -1543,11 +1548,13 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
 // the shading of the wavefront kernels (shade_vertex) and the traversal inline (trace_ray: the closest
 // hit of each extension ray and the any-hit test of each shadow ray, which adds an unoccluded
 // contribution to the film). Every path follows the same Philox draws and traversal as in the
-// wavefront, so the film is the same up to the order of its FP64 sums.
+// wavefront, so the film is the same up to the order of its FP64 sums. BATCH: each path renders with
+// its own job's scene, parameters, film and renderer.
 constexpr int kFinishBlock = 128;
 constexpr int kFinishMaxVertices = 4096;
-template <typename R, bool DIRECT>
-__global__ void __launch_bounds__(kFinishBlock) k_finish(SceneView<R> sv, WaveView<R> w, RenderConsts rc) {
+template <typename R, bool DIRECT, bool BATCH>
+__global__ void __launch_bounds__(kFinishBlock)
+    k_finish(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0, const JobView<R>* __restrict__ jobs) {
     NGI_COUNTS_DECL
     block_counts_init(bc);
     __shared__ unsigned long long blk_ext, blk_sh;
@@ -1558,6 +1565,11 @@ __global__ void __launch_bounds__(kFinishBlock) k_finish(SceneView<R> sv, WaveVi
     const int n = min(*w.ext_count, w.Q);
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
         const int s = w.ext_queue[item];
+        const int job = BATCH ? w.job[s] : 0;
+        const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
+        const RenderConsts& rc = BATCH ? jobs[job].rc : rc0;
+        double* const film = BATCH ? jobs[job].film : w.film;
+        const bool direct = BATCH ? rc.renderer == NGI_RENDERER_PTDIRECT : DIRECT;
         float4 h = w.hit[s];
         uint4 pa = make_uint4(0u, 0u, 0u, 0u), pb = pa;
         // a path ends by Russian roulette with probability 1/2 per vertex; the cap only bounds the loop
@@ -1567,7 +1579,7 @@ __global__ void __launch_bounds__(kFinishBlock) k_finish(SceneView<R> sv, WaveVi
                 break;
             }
             const bool alive = shade_vertex<R, false>(
-                sv, rc, w.film, DIRECT, w, s, h, pa, pb, nullptr, bc, [&](const ShadowRay<R>& sa, int, int) {
+                sv, rc, film, direct, w, s, h, pa, pb, nullptr, bc, [&](const ShadowRay<R>& sa, int, int) {
                     if (!sa.valid) return;
                     float tmax = sa.tmax, u = 0.0f, v = 0.0f;
                     const int occ = trace_ray<true, false>(sv.nodes, sv.tris, sv.num_nodes, sa.ox, sa.oy, sa.oz, sa.dx,
@@ -1575,7 +1587,7 @@ __global__ void __launch_bounds__(kFinishBlock) k_finish(SceneView<R> sv, WaveVi
                     n_sh++;
                     if (occ >= 0) return;
                     if (finite3(sa.c)) {
-                        film_add(w.film, sa.pixel, sa.c);
+                        film_add(film, sa.pixel, sa.c);
                         atomicAdd(&bc.contrib, 1u);
                     } else {
                         atomicAdd(&bc.nonfinite, 1u);
@@ -2084,9 +2096,10 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     }
     cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
     double kms[2] = {0, 0};
-    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, outside batches, the
-    // adjoint and the measurement renders (which time or count the wavefront kernels themselves)
-    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !BATCH && !STATS;
+    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders and
+    // batches, outside the adjoint and the measurement renders (which time or count the wavefront
+    // kernels themselves)
+    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !STATS;
     const int finish_max = std::max(v.Q / 32, 4096);
     long long finish_paths = 0;
     long long launches = 0;
@@ -2133,8 +2146,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
                 if (!kernel_timing && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples &&
                     pending <= finish_max) {
                     if (pending > 0) {
-                        k_finish<R, DIRECT><<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, 0, stream>>>(
-                            sv, v, rc);
+                        k_finish<R, DIRECT, BATCH>
+                            <<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, 0, stream>>>(sv, v, rc, jobs);
                         CUDA_CHECK(cudaGetLastError());
                         CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                                    stream));
