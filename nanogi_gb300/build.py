@@ -49,13 +49,22 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+# render.cu: FP32 division and square root as the hardware approximations (within 2 ulp) instead of
+# the IEEE-rounded sequences. This changes the FP32 shading arithmetic only: the traversal and the
+# watertight triangle test are written with explicit round-to-nearest intrinsics (__fdiv_rn,
+# __fmul_rn, __frcp_rn), which the flags leave alone, and FP64 arithmetic is unaffected. Measured on
+# the 1.55M-triangle terrain: path-logic launches 0.261 -> 0.242 ms, 15.04 -> 14.71 ms per 16-spp
+# render; Cornell box 4357 -> 4482 Mrays/s.
+CUDA_FLAGS = {"render.cu": ["-prec-div=false", "-prec-sqrt=false"]}
+
+
 def _compile(src: Path, obj: Path, headers: list[Path]) -> Path:
-    if not _stale(obj, [src] + headers):
+    if not _stale(obj, [src, Path(__file__)] + headers):
         return obj
     inc = ["-I", str(CSRC), "-I", str(ROOT / "include")]
     if src.suffix == ".cu":
-        cmd = [NVCC, "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fvisibility=hidden",
-               *inc, "-c", str(src), "-o", str(obj)]
+        cmd = [NVCC, "-std=c++17", "-O3", "-lineinfo", *CUDA_FLAGS.get(src.name, []), *ARCH, "-Xcompiler",
+               "-fPIC,-fvisibility=hidden", *inc, "-c", str(src), "-o", str(obj)]
     else:
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra",
                "-I", str(CUDA_HOME / "include"), *inc, "-c", str(src), "-o", str(obj)]
