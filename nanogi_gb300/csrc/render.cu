@@ -1552,6 +1552,11 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
 // its own job's scene, parameters, film and renderer.
 constexpr int kFinishBlock = 128;
 constexpr int kFinishMaxVertices = 4096;
+// Paths left in flight below which the wave hands them to k_finish: its time grows with the paths it
+// gets (the longest of them sets it), while one more drain iteration costs a full set of launches.
+// Terrain, ptdirect, 2^25-slot wave: 8192 paths 14.59 ms per 16-spp render, 32768 14.43, 131072
+// 14.36; per 64-spp render 55.33, 55.10 and 54.89 ms.
+constexpr int kFinishMaxPaths = 131072;
 template <typename R, bool DIRECT, bool BATCH>
 __global__ void __launch_bounds__(kFinishBlock)
     k_finish(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0, const JobView<R>* __restrict__ jobs) {
@@ -2078,11 +2083,15 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     }
 
     trace_grid<R, STATS, ADJ, BATCH>();
-    cudaGraphExec_t exec = nullptr;
-    if (!kernel_timing) {
+    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders and
+    // batches, outside the adjoint and the measurement renders (which time or count the wavefront
+    // kernels themselves)
+    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !STATS;
+    auto capture = [&](int n) {
         cudaGraph_t graph = nullptr;
+        cudaGraphExec_t e = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < iters_per_graph; it++)
+        for (int it = 0; it < n; it++)
             enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LOGIC>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
                                                                    nullptr, jobs, num_jobs, it & 1);
         const cudaError_t cap = cudaStreamEndCapture(stream, &graph);
@@ -2090,17 +2099,30 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
             if (graph) cudaGraphDestroy(graph);
             throw DeviceError(std::string("graph capture failed: ") + cudaGetErrorString(cap));
         }
-        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        const cudaError_t inst = cudaGraphInstantiate(&e, graph, 0);
         cudaGraphDestroy(graph);
         if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
+        return e;
+    };
+    // Once every sample is claimed, the wave drains: the host then reads the counters after every
+    // drain graph (two iterations, one outside compacted shading) so that the wave-end launch starts
+    // as soon as few paths remain, instead of at the next multiple of iters_per_graph.
+    const int drain_iters = compact ? 2 : 1;
+    cudaGraphExec_t exec = nullptr, exec_drain = nullptr;
+    if (!kernel_timing) {
+        exec = capture(iters_per_graph);
+        if (finish && drain_iters < iters_per_graph) {
+            try {
+                exec_drain = capture(drain_iters);
+            } catch (...) {
+                cudaGraphExecDestroy(exec);
+                throw;
+            }
+        }
     }
     cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
     double kms[2] = {0, 0};
-    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders and
-    // batches, outside the adjoint and the measurement renders (which time or count the wavefront
-    // kernels themselves)
-    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !STATS;
-    const int finish_max = std::max(v.Q / 32, 4096);
+    bool draining = false;
     long long finish_paths = 0;
     long long launches = 0;
 
@@ -2130,8 +2152,8 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
                 launches++;
                 iterations++;
             } else {
-                CUDA_CHECK(cudaGraphLaunch(exec, stream));
-                iterations += iters_per_graph;
+                CUDA_CHECK(cudaGraphLaunch(draining ? exec_drain : exec, stream));
+                iterations += draining ? drain_iters : iters_per_graph;
             }
             CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost, stream));
             CUDA_CHECK(cudaStreamSynchronize(stream));
@@ -2143,8 +2165,9 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
             if constexpr (finish) {
                 // every sample claimed and few paths left: run them to their end in one launch
                 const int pending = wv->h_ctr->ext_count;
-                if (!kernel_timing && wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples &&
-                    pending <= finish_max) {
+                const bool claimed = wv->h_ctr->next_sample >= (unsigned long long)rc.num_samples;
+                if (claimed && exec_drain) draining = true;
+                if (!kernel_timing && claimed && pending <= kFinishMaxPaths) {
                     if (pending > 0) {
                         k_finish<R, DIRECT, BATCH>
                             <<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, 0, stream>>>(sv, v, rc, jobs);
@@ -2167,11 +2190,13 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     } catch (...) {
         cudaStreamSynchronize(stream);
         if (exec) cudaGraphExecDestroy(exec);
+        if (exec_drain) cudaGraphExecDestroy(exec_drain);
         for (auto& e : kev)
             if (e) cudaEventDestroy(e);
         throw;
     }
     if (exec) cudaGraphExecDestroy(exec);
+    if (exec_drain) cudaGraphExecDestroy(exec_drain);
     for (auto& e : kev)
         if (e) cudaEventDestroy(e);
     float ms = 0;
@@ -2250,13 +2275,20 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     ds.last_stats = ngi_render_stats{};
     if (p.num_samples == 0) return;
     const bool bdpt = p.renderer == NGI_RENDERER_BDPT;
-    // 2^23 path slots (~0.9 GB FP32): on the terrain 1356 Mrays/s against 1322 at 2^22 and 1318
-    // at 2^24 (2100 against 2082 and 2025 at 2^22 / 2^21 with the current kernels). bdpt keeps
-    // 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): 2^18. A smaller default for scenes
-    // with a small BVH (2^20 below 32 MB) was measured and not kept: the Cornell box bench ran at
-    // 4995 against 4050 Mrays/s, but its convergence study took 0.253 against 0.225 s and the
-    // 256-job batch rendered one job at a time 3719 against 4431 Mrays/s.
-    int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (1 << 23));
+    // Path slots of the wave (never more than the render's samples). A slot takes about 257 B in
+    // FP32 (101 B of path state, three shadow-ray entries) and 400 B in FP64. ptdirect: 2^25
+    // (8.6 GB FP32). Each iteration pays a fixed tail (the slowest ray of its traversal launch, the
+    // ramp of its logic launches), which a larger wave spreads over more rays, and its shading
+    // visits only queued slots. Terrain, with the wave-end launch: 14.75 ms per 16-spp render at
+    // 2^23, 14.36 at 2^25 (every sample in flight at once); 65.5 against 54.9 ms per 64-spp render.
+    // pt, lt and ltdirect keep 2^23: their logic kernel visits every slot of the wave in each
+    // iteration, so a larger wave costs them in the drain (Cornell box, pt: 0.264 s to 1% error at
+    // 2^25 against 0.23 s). bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64):
+    // 2^18. A smaller default for scenes with a small BVH (2^20 below 32 MB) was measured and not
+    // kept: the Cornell box bench ran at 4995 against 4050 Mrays/s, but its convergence study took
+    // 0.253 against 0.225 s and the 256-job batch rendered one job at a time 3719 against 4431 Mrays/s.
+    const bool compacted = p.renderer == NGI_RENDERER_PTDIRECT;
+    int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (compacted ? (1 << 25) : (1 << 23)));
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
     Q = (Q + 255) / 256 * 256;
@@ -2644,7 +2676,7 @@ void render_batch(std::vector<HostScene*>& scenes, const std::vector<ngi_render_
             };
             measure(cfg);  // warm: kernels, graphs, wave allocation
             double best = measure(cfg);
-            const int waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+            const int waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25};
             for (int wv : waves) {
                 if (wv == cfg.wave || wv > std::max<long long>(trial_total, 256) * 2) continue;
                 BatchConfig c = cfg;
