@@ -70,6 +70,7 @@ struct WaveCounters {
     int error_flags;                  // bit 0: traversal stack overflow, 1: adjoint prefix, 2: wave-end vertex cap
     int ext_count_b;                  // compacted shading: count of the second extension queue
     int carry_count[2];               //   and of the two carry queues (reset per iteration by parity)
+    int regen_seed;                   //   and the regeneration queue's length in the first iteration
     unsigned long long stat_camera;
     unsigned long long stat_ext;
     unsigned long long stat_shadow;
@@ -777,9 +778,10 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
         if constexpr (PART == kLogicShadeQ) {
             // ---- hand the slots whose path ended to the regeneration kernel, queue the continuing
             // paths' rays and the staged shadow rays: one atomic per queue for the whole block ----
+            // (the slot state array is not written: compacted shading knows a slot's state from the
+            // queue it comes from, and only the fused kernel reads the array)
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
-            if (valid) w.state[s] = st;
             const unsigned mr = __ballot_sync(0xFFFFFFFFu, need_new), me = __ballot_sync(0xFFFFFFFFu, want_ext);
             const int warp = (int)(threadIdx.x >> 5);
             if (lane_id() == 0) {
@@ -940,7 +942,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             }
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
-            if (valid) w.state[s] = st;
+            if (PART == kLogicFused && valid) w.state[s] = st;  // read only by the fused kernel
             {
                 // compacted shading visits only queued slots: one left empty waits in the carry queue
                 const bool carry = PART == kLogicRegen && w.carry_out && valid && st == SLOT_EMPTY;
@@ -2007,17 +2009,23 @@ __global__ void k_iteration_begin(WaveCounters* ctr, int parity) {
     ctr->active = 0;
     ctr->ext_fetch = 0;
     ctr->sh_fetch = 0;
-    ctr->regen_count = 0;
+    ctr->regen_count = ctr->regen_seed;  // the wave's slots in its first iteration, then 0
+    ctr->regen_seed = 0;
     if (parity) ctr->ext_count = 0;
     else ctr->ext_count_b = 0;
     ctr->carry_count[1 - parity] = 0;
 }
 
-// Every slot of a new wave starts empty, in the carry queue the first iteration reads.
-__global__ void k_wave_init_carry(int* carry, int Q, WaveCounters* ctr) {
+// Every slot of a new wave starts empty, in the regeneration queue of the first iteration: its
+// shading launch has no queued slot, and regeneration starts a sample in every slot. (Handing the
+// slots through the carry queue instead took the first shading launch 0.28 ms for 2^25 slots.)
+__global__ void k_wave_init_slots(int* regen_queue, int Q, WaveCounters* ctr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < Q) carry[i] = i;
-    if (i == 0) ctr->carry_count[0] = Q;
+    if (i < Q) regen_queue[i] = i;
+    if (i == 0) {
+        ctr->regen_seed = Q;
+        ctr->carry_count[0] = 0;
+    }
 }
 
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
@@ -2077,7 +2085,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
     constexpr bool compact = compact_shading<DIRECT, BATCH, LOGIC>();
     if constexpr (compact) {
-        k_wave_init_carry<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.carry_a, v.Q, wv->ctr);
+        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, wv->ctr);
         CUDA_CHECK(cudaGetLastError());
         iters_per_graph += iters_per_graph & 1;  // queue parity must restart at 0 with every graph launch
     }
@@ -2850,7 +2858,7 @@ void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, int 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(v.ctr, 0, sizeof(WaveCounters), stream));
     if constexpr (compact_shading<DIRECT, false, kLogicCamera>())
-        k_wave_init_carry<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.carry_a, v.Q, v.ctr);
+        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, v.ctr);
     const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
     const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
     WaveCounters h{};
