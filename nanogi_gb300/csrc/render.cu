@@ -38,6 +38,17 @@ namespace ngi {
     } while (0)
 
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
+// Loads of wave records the traversal reads once per iteration, with the cache-streaming hint
+// (evict first), so that L2 keeps the BVH nodes and triangles the rays share.
+template <typename R>
+__device__ __forceinline__ Vec4T<R> ld_stream(const Vec4T<R>* p) {
+    if constexpr (sizeof(R) == 4) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+        return Vec4T<R>{v.x, v.y, v.z, v.w};
+    } else {
+        return *p;
+    }
+}
 
 // Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
 // FP32 logic at 128 registers (25% occupancy); 4 caps it at 64 registers with ~250 B of spills
@@ -1473,13 +1484,13 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
                     item = shadow ? i - n_ext : i;
                     float4 o, d;
                     if (shadow) {
-                        o = w.sh_o[item];
-                        d = w.sh_d[item];
+                        o = __ldcs(w.sh_o + item);
+                        d = __ldcs(w.sh_d + item);
                         if (BATCH) job = w.sh_job[item];
                     } else {
-                        slot = w.ext_queue[item];
-                        o = w.ray_o[slot];
-                        d = w.ray_d[slot];
+                        slot = __ldcs(w.ext_queue + item);
+                        o = __ldcs(w.ray_o + slot);
+                        d = __ldcs(w.ray_d + slot);
                         if (BATCH) job = w.job[slot];
                     }
                     if (BATCH) {
@@ -1499,10 +1510,10 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
             if (done) {
                 if (shadow) {
                     if (s.hit < 0) {
-                        const Vec4T<R> c = w.sh_c[item];
+                        const Vec4T<R> c = ld_stream(w.sh_c + item);
                         const V3<R> cc = v3<R>(c.x, c.y, c.z);
                         if (finite3(cc)) {
-                            const uint32_t pix = w.sh_pix[item];
+                            const uint32_t pix = __ldcs(w.sh_pix + item);
                             film_add(BATCH ? jobs[job].film : w.film, pix, cc);
                             atomicAdd(&blk_contrib, 1u);
                             if (ADJ) {
@@ -1521,7 +1532,7 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
                         }
                     }
                 } else {
-                    w.hit[slot] = make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit));
+                    __stcs(w.hit + slot, make_float4(s.tmax, s.hu, s.hv, __int_as_float(s.hit)));
                 }
                 item = -1;
             }
