@@ -1562,7 +1562,9 @@ __global__ void __launch_bounds__(128, kTraceMinBlocks) k_trace(SceneView<R> sv,
 // hit of each extension ray and the any-hit test of each shadow ray, which adds an unoccluded
 // contribution to the film). Every path follows the same Philox draws and traversal as in the
 // wavefront, so the film is the same up to the order of its FP64 sums. BATCH: each path renders with
-// its own job's scene, parameters, film and renderer.
+// its own job's scene, parameters, film and renderer. ADJ: the backward pass; an unoccluded shadow
+// ray also adds its gradients (adj_accumulate with the path's prefix at that vertex, as the traversal
+// kernel does from the shadow queue), summed per block in shared memory when the scene is small.
 constexpr int kFinishBlock = 128;
 constexpr int kFinishMaxVertices = 4096;
 // Paths left in flight below which the wave hands them to k_finish: its time grows with the paths it
@@ -1570,11 +1572,14 @@ constexpr int kFinishMaxVertices = 4096;
 // Terrain, ptdirect, 2^25-slot wave: 8192 paths 14.59 ms per 16-spp render, 32768 14.43, 131072
 // 14.36; per 64-spp render 55.33, 55.10 and 54.89 ms.
 constexpr int kFinishMaxPaths = 131072;
-template <typename R, bool DIRECT, bool BATCH>
+template <typename R, bool DIRECT, bool BATCH, bool ADJ>
 __global__ void __launch_bounds__(kFinishBlock)
     k_finish(SceneView<R> sv0, WaveView<R> w, RenderConsts rc0, const JobView<R>* __restrict__ jobs) {
     NGI_COUNTS_DECL
     block_counts_init(bc);
+    extern __shared__ float adj_smem_finish[];
+    float* gsm = (ADJ && rc0.num_prims <= kAdjSmemPrims) ? adj_smem_finish : nullptr;
+    if (ADJ) adj_smem_clear(gsm, rc0.num_prims);
     __shared__ unsigned long long blk_ext, blk_sh;
     if (threadIdx.x == 0) blk_ext = blk_sh = 0ull;
     __syncthreads();
@@ -1596,8 +1601,8 @@ __global__ void __launch_bounds__(kFinishBlock)
                 atomicOr(&w.ctr->error_flags, 4);
                 break;
             }
-            const bool alive = shade_vertex<R, false>(
-                sv, rc, film, direct, w, s, h, pa, pb, nullptr, bc, [&](const ShadowRay<R>& sa, int, int) {
+            const bool alive = shade_vertex<R, ADJ>(
+                sv, rc, film, direct, w, s, h, pa, pb, gsm, bc, [&](const ShadowRay<R>& sa, int count, int vprim) {
                     if (!sa.valid) return;
                     float tmax = sa.tmax, u = 0.0f, v = 0.0f;
                     const int occ = trace_ray<true, false>(sv.nodes, sv.tris, sv.num_nodes, sa.ox, sa.oy, sa.oz, sa.dx,
@@ -1607,6 +1612,8 @@ __global__ void __launch_bounds__(kFinishBlock)
                     if (finite3(sa.c)) {
                         film_add(film, sa.pixel, sa.c);
                         atomicAdd(&bc.contrib, 1u);
+                        if (ADJ) adj_accumulate(w, sv, sa.pixel, sa.c, pa, pb, count, vprim, sa.light_prim, gsm,
+                                                rc.num_prims);
                     } else {
                         atomicAdd(&bc.nonfinite, 1u);
                     }
@@ -1623,6 +1630,7 @@ __global__ void __launch_bounds__(kFinishBlock)
     if (n_ext) atomicAdd(&blk_ext, (unsigned long long)n_ext);
     if (n_sh) atomicAdd(&blk_sh, (unsigned long long)n_sh);
     if (overflow) atomicOr(&w.ctr->error_flags, 1);
+    if (ADJ) adj_flush(w, gsm, rc0.num_prims);  // synchronises the block first
     block_counts_flush(bc, w.ctr);  // synchronises the block first
     if (threadIdx.x == 0) {
         if (blk_ext) atomicAdd(&w.ctr->stat_ext, blk_ext);
@@ -2102,10 +2110,9 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     }
 
     trace_grid<R, STATS, ADJ, BATCH>();
-    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders and
-    // batches, outside the adjoint and the measurement renders (which time or count the wavefront
-    // kernels themselves)
-    constexpr bool finish = LOGIC == kLogicCamera && !ADJ && !STATS;
+    // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders, batches
+    // and the adjoint, outside the measurement renders (which time or count the wavefront kernels)
+    constexpr bool finish = LOGIC == kLogicCamera && !STATS;
     auto capture = [&](int n) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t e = nullptr;
@@ -2188,13 +2195,18 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
                 if (claimed && exec_drain) draining = true;
                 if (!kernel_timing && claimed && pending <= kFinishMaxPaths) {
                     if (pending > 0) {
-                        k_finish<R, DIRECT, BATCH>
-                            <<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, 0, stream>>>(sv, v, rc, jobs);
+                        const size_t finish_smem =
+                            (ADJ && rc.num_prims <= kAdjSmemPrims) ? 6 * sizeof(float) * rc.num_prims : 0;
+                        k_finish<R, DIRECT, BATCH, ADJ>
+                            <<<(pending + kFinishBlock - 1) / kFinishBlock, kFinishBlock, finish_smem, stream>>>(
+                                sv, v, rc, jobs);
                         CUDA_CHECK(cudaGetLastError());
                         CUDA_CHECK(cudaMemcpyAsync(wv->h_ctr, wv->ctr, sizeof(WaveCounters), cudaMemcpyDeviceToHost,
                                                    stream));
                         CUDA_CHECK(cudaStreamSynchronize(stream));
                         if (wv->h_ctr->error_flags & 1) throw DeviceError("traversal stack overflow", NGI_ERR_UNSUPPORTED);
+                        if (wv->h_ctr->error_flags & 2)
+                            throw DeviceError("adjoint path longer than 16 surface vertices", NGI_ERR_UNSUPPORTED);
                         if (wv->h_ctr->error_flags & 4)
                             throw DeviceError("a path outran the wave-end vertex cap", NGI_ERR_DEVICE_TIMEOUT);
                         finish_paths = pending;
@@ -2545,14 +2557,16 @@ void DeviceRenderBackward(HostScene& hs, const ngi_render_params& p, const doubl
         const double scale = (double)p.width * (double)p.height / (double)p.num_samples;
         k_scale<<<grid_for((int)std::min<size_t>(elems, 1u << 30), 256), 256, 0, stream>>>(ds.adj, elems, scale);
         CUDA_CHECK(cudaGetLastError());
-        int Q = p.wave_size > 0 ? p.wave_size : (1 << 22);
+        // ptdirect: the forward render's 2^25 slots (the inverse box, 512x512 at 64 spp: backward
+        // 9.93 ms with every sample in flight against 11.32 ms at 2^22); pt keeps 2^22
+        const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
+        int Q = p.wave_size > 0 ? p.wave_size : (direct ? (1 << 25) : (1 << 22));
         const long long need = std::max<long long>(p.num_samples, 256);
         if ((long long)Q > need) Q = (int)need;
         Q = (Q + 255) / 256 * 256;
         RenderWave* wv = ensure_wave(ds, Q, p.precision);
         const RenderConsts rc = consts_of(p, (int)hs.prims.size());
         const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
-        const bool direct = p.renderer == NGI_RENDERER_PTDIRECT;
         if (p.precision == NGI_PRECISION_FP64) {
             WaveView<double>& v = wv->vd;
             v.film = ds.film;
