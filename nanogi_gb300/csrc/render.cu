@@ -2015,6 +2015,9 @@ int trace_grid() {
 // logic kernels' time per iteration stayed at 0.34 ms (a miss costs shading little: one hit
 // record read and a queue append), while the traversal launch grew from 0.613 to 0.644 ms:
 // 1741 against 1791 Mrays/s on the terrain.
+// Batches keep the fused kernel: compacted, with each slot's job choosing its renderer at run time,
+// the 256-job batch took 2,000 against 1,245 ms (the split kernels spill 188 B per thread with the
+// job lookups, and the batch's shadow rays cannot be staged without their job).
 template <bool DIRECT, bool BATCH, int LOGIC>
 constexpr bool compact_shading() {
     return DIRECT && !BATCH && LOGIC == kLogicCamera;
