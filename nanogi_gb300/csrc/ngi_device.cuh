@@ -65,7 +65,7 @@ struct DevLight {
     int tri_count;
     int tri_base;      // first triangle of this light's mesh in the emitter arrays
     int cdf_offset;    // index of this light's first cdf entry in the shared cdf array
-    int pad;
+    int sensor_facing; // 0: every triangle faces away from the pinhole eye (no sensor connection)
     V3<R> Le;
     R inv_area;
     V3<R> position;    // point light

@@ -495,6 +495,7 @@ NGI_D void next_event(const SceneView<R>& sv, const RenderConsts& rc, const Geom
     li = li < 0 ? 0 : (li > nl - 1 ? nl - 1 : li);
     const DevLight<R>& L = sv.lights[li];
     if (L.type == LT_DIRECTIONAL) return;  // Le is 0 without forceDegenerated (rt.hpp:934-937)
+    if (at_sensor && !L.sensor_facing) return;  // every point of L faces away from the pinhole eye
     Geom<R> gl;
     R pdf_pos;
     if (L.type == LT_AREA) {
@@ -1759,6 +1760,32 @@ void build_tables(const HostScene& hs, std::vector<DevMaterial<R>>& mats, std::v
             sensor.tri_count = (int)p.tri_count;
             add_emitter_mesh(p, sensor.tri_base, sensor.cdf_offset);
         }
+    }
+    // Next-event estimation at a pinhole sensor connects the eye to a point of the light, and an area
+    // light contributes only from the side its normal faces (rt.hpp:917-937). A light all of whose
+    // triangles face away from the eye never contributes there, so that estimation stops at the pick
+    // (the film is the same: the facing test would reject every sample). The eye must lie behind each
+    // triangle's plane by 1e-4 of its distance, far beyond the FP32 rounding of the facing test.
+    for (size_t li = 0; li < hs.light_prims.size(); li++) {
+        DevLight<R>& L = lights[li];
+        L.sensor_facing = 1;
+        if (sensor.type != E_PINHOLE || L.type != L_AREA) continue;
+        const HostPrimitive& p = hs.prims[hs.light_prims[li]];
+        bool away = p.tri_count > 0;
+        for (int64_t t = 0; t < p.tri_count && away; t++) {
+            const float* P = hs.tri_pos.data() + 9 * (p.tri_first + t);
+            const double e1[3] = {(double)P[3] - P[0], (double)P[4] - P[1], (double)P[5] - P[2]};
+            const double e2[3] = {(double)P[6] - P[0], (double)P[7] - P[1], (double)P[8] - P[2]};
+            const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                 e1[0] * e2[1] - e1[1] * e2[0]};
+            const double* eye = hs.prims[hs.sensor_prim].eye;
+            const double v[3] = {eye[0] - P[0], eye[1] - P[1], eye[2] - P[2]};
+            const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            const double vv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const double d = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+            away = nn > 0.0 && vv > 0.0 && d < -1e-4 * nn * vv;
+        }
+        if (away) L.sensor_facing = 0;
     }
 }
 
