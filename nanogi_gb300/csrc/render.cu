@@ -38,8 +38,8 @@ namespace ngi {
     } while (0)
 
 template <typename R> struct alignas(4 * sizeof(R)) Vec4T { R x, y, z, w; };
-// Loads of wave records the traversal reads once per iteration, with the cache-streaming hint
-// (evict first), so that L2 keeps the BVH nodes and triangles the rays share.
+// Wave records written and read once per iteration (rays, hits, shadow rays) move with the
+// cache-streaming hint (evict first), so that L2 keeps the BVH nodes and triangles the rays share.
 template <typename R>
 __device__ __forceinline__ Vec4T<R> ld_stream(const Vec4T<R>* p) {
     if constexpr (sizeof(R) == 4) {
@@ -48,6 +48,11 @@ __device__ __forceinline__ Vec4T<R> ld_stream(const Vec4T<R>* p) {
     } else {
         return *p;
     }
+}
+template <typename R>
+__device__ __forceinline__ void st_stream(Vec4T<R>* p, const Vec4T<R>& v) {
+    if constexpr (sizeof(R) == 4) __stcs(reinterpret_cast<float4*>(p), make_float4(v.x, v.y, v.z, v.w));
+    else *p = v;
 }
 
 // Resident 256-thread blocks per SM the path-logic kernel is compiled for. 2 leaves ptdirect's
@@ -448,10 +453,10 @@ NGI_D void emit_shadow(const WaveView<R>& w, const ShadowRay<R>& sr, int job, co
                        int count, int vprim) {
     const int q = coalesced_append(&w.ctr->sh_count, sr.valid);
     if (!sr.valid) return;
-    w.sh_o[q] = make_float4(sr.ox, sr.oy, sr.oz, sr.tmin);
-    w.sh_d[q] = make_float4(sr.dx, sr.dy, sr.dz, sr.tmax);
-    w.sh_c[q] = Vec4T<R>{sr.c.x, sr.c.y, sr.c.z, R(0)};
-    w.sh_pix[q] = sr.pixel;
+    __stcs(w.sh_o + q, make_float4(sr.ox, sr.oy, sr.oz, sr.tmin));
+    __stcs(w.sh_d + q, make_float4(sr.dx, sr.dy, sr.dz, sr.tmax));
+    st_stream(w.sh_c + q, Vec4T<R>{sr.c.x, sr.c.y, sr.c.z, R(0)});
+    __stcs(w.sh_pix + q, sr.pixel);
     if (BATCH) w.sh_job[q] = job;
     if (ADJ) {
         if (count > 0) {
@@ -546,8 +551,8 @@ template <typename R>
 NGI_D void store_ray(const WaveView<R>& w, int s, const Geom<R>& g, V3<R> d, int mode) {
     const V3<R> o = g.p;
     const float4 ro = ray_origin(g, d, mode);
-    w.ray_o[s] = ro;
-    w.ray_d[s] = make_float4((float)d.x, (float)d.y, (float)d.z, kInfF);
+    __stcs(w.ray_o + s, ro);
+    __stcs(w.ray_d + s, make_float4((float)d.x, (float)d.y, (float)d.z, kInfF));
     if (sizeof(R) == 8) {
         // the hit point is reconstructed from the origin the ray was traced from
         if (mode == NGI_RAY_OFFSET_SCALED) w.od_o[s] = Vec4T<double>{(double)ro.x, (double)ro.y, (double)ro.z, 0.0};
@@ -572,7 +577,7 @@ NGI_D int hit_geometry(const SceneView<R>& sv, const RenderConsts& rc, const Wav
         o = v3<R>((R)a.x, (R)a.y, (R)a.z);
         d = v3<R>((R)b.x, (R)b.y, (R)b.z);
     } else {
-        const float4 a = w.ray_o[s], b = w.ray_d[s];
+        const float4 a = __ldcs(w.ray_o + s), b = __ldcs(w.ray_d + s);
         o = v3<R>((R)a.x, (R)a.y, (R)a.z);
         d = v3<R>((R)b.x, (R)b.y, (R)b.z);
     }
@@ -710,6 +715,8 @@ constexpr int kRegenAttempts = 2;  // samples a slot may claim per iteration
 constexpr size_t kShadowPerSlot = 1 + (kRegenAttempts > 1 ? kRegenAttempts : 1);
 // Resident blocks per SM the two ptdirect halves are compiled for (64 registers each). 5 or 6
 // blocks (48 / 40 registers) were slower on the terrain: 2066-2083 against 2103 Mrays/s.
+// (3 blocks for the shading kernel, about 85 registers and fewer spills with the fast FP32 division:
+// 13.83 against 13.55 ms per 16-spp terrain render)
 constexpr int kShadeMinBlocks = 4, kRegenMinBlocks = 4;
 // Measured and not kept: sorting each block's 256 items by class (BSDF of the hit primitive,
 // miss, empty slot) in shared memory before shading: 1798-1802 against 1803-1804 Mrays/s on the
@@ -768,7 +775,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
         if (PART != kLogicRegen && st == SLOT_ACTIVE) {
             // ---- consume the extension hit (src/nanogi.cpp:557-603 / 767-799) ----
             bool alive = false;
-            const float4 h = w.hit[s];
+            const float4 h = __ldcs(w.hit + s);
             if (__float_as_int(h.w) >= 0) {
                 const int job = BATCH ? w.job[s] : 0;
                 const SceneView<R>& sv = BATCH ? jobs[job].sv : sv0;
@@ -825,10 +832,10 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
                 const StagedShadow<R>* stage = shadow_stage<R>();
                 for (int t = (int)threadIdx.x; t < s_staged_n; t += kLogicBlock) {
                     const int q = s_staged_base + t;
-                    w.sh_o[q] = stage[t].o;
-                    w.sh_d[q] = stage[t].d;
-                    w.sh_c[q] = stage[t].c;
-                    w.sh_pix[q] = stage[t].pixel;
+                    __stcs(w.sh_o + q, stage[t].o);
+                    __stcs(w.sh_d + q, stage[t].d);
+                    st_stream(w.sh_c + q, stage[t].c);
+                    __stcs(w.sh_pix + q, stage[t].pixel);
                 }
             }
             __syncthreads();  // the scratch and the stage are reused by the next item
