@@ -116,17 +116,25 @@ def bounce_rays(rays: np.ndarray, prim: np.ndarray, t: np.ndarray, rng, tmin: fl
 
 
 T_REL_TOL = 1e-5  # hit-distance tolerance
+# Two coplanar or touching triangles at a ray's hit return distances that differ by the rounding
+# of the watertight test, which scales with the coordinates of the vertices and the ray origin, not
+# with the distance: for a ray leaving a floor 1.5 mm below it, at coordinates near 3, that is a
+# relative difference of about 2e-5. With the rays given, a tie may also differ by this many units
+# of those coordinates' magnitude (a few FP32 ulps).
+T_COORD_TOL = 4e-7
 
 
-def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999):
+def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999, rays=None):
     """First hits of the GPU traversal against the oracle's for the same rays.
 
     Hit / miss agree and primitive ids are bit-exact, except on ties: rays whose two answers lie
-    at the same distance to within T_REL_TOL (coincident surfaces, such as a box standing on a
-    floor or two triangles sharing the edge the ray hits, where the watertight test's rounding or
-    the traversal order picks one of them); ties must stay below `max_tie_share`. Hit distances
-    are within T_REL_TOL everywhere and bit-identical on at least `min_exact` of the rays where
-    the ids agree; barycentrics agree to 1e-6 there. Returns (hit rays compared, ties)."""
+    at the same distance to within T_REL_TOL (or, given the rays, within T_COORD_TOL of the
+    magnitude of the ray origin and hit point coordinates): coincident surfaces, such as a box
+    standing on a floor, two overlapping coplanar triangles or two triangles sharing the edge the
+    ray hits, where the watertight test's rounding or the traversal order picks one of them. Ties
+    must stay below `max_tie_share`. Hit distances are within T_REL_TOL everywhere and
+    bit-identical on at least `min_exact` of the rays where the ids agree; barycentrics agree to
+    1e-6 there. Returns (hit rays compared, ties)."""
     gp, gt, guv = gpu
     op, ot, ouv = ora
     miss_agree = (gp < 0) == (op < 0)
@@ -134,12 +142,19 @@ def check_hits(gpu, ora, label, max_tie_share=0.01, min_exact=0.999):
     both = (gp >= 0) & (op >= 0)
     same = gp[both] == op[both]
     tie = ~same
-    rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
-    bad = tie & (rel > T_REL_TOL)
+    diff = np.abs(gt[both].astype(np.float64) - ot[both])
+    rel = diff / np.maximum(np.abs(ot[both]), 1e-30)
+    tie_window = T_REL_TOL * np.abs(ot[both]).astype(np.float64)
+    if rays is not None:
+        r = np.asarray(rays, np.float64)[both]
+        hit = r[:, 0:3] + r[:, 4:7] * ot[both, None].astype(np.float64)
+        coord = np.maximum(np.abs(r[:, 0:3]).max(1), np.abs(hit).max(1))
+        tie_window = np.maximum(tie_window, T_COORD_TOL * coord)
+    bad = tie & (diff > tie_window)
     assert not bad.any(), (f"{label}: {bad.sum()} rays hit different primitives at different distances, e.g. "
                            f"gpu t={gt[both][bad][:3]} oracle t={ot[both][bad][:3]}")
     assert tie.mean() <= max_tie_share, f"{label}: {tie.sum()} of {both.sum()} rays resolve a tie differently"
-    assert rel.max(initial=0.0) <= T_REL_TOL, f"{label}: max rel t error {rel.max()}"
+    assert rel[same].max(initial=0.0) <= T_REL_TOL, f"{label}: max rel t error {rel[same].max()}"
     exact = (gt[both][same] == ot[both][same]).mean() if same.any() else 1.0
     assert exact >= min_exact, f"{label}: only {exact:.6f} of hit distances are bit-identical"
     if same.any():

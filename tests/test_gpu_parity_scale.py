@@ -87,7 +87,7 @@ def _check_scene(desc, scene, ora, aspect, lo, hi, n_camera, n_random, n_brute, 
     sets = _ray_set(desc, ora, aspect, lo, hi, n_camera, n_random, seed)
     total = 0
     for name, rays in sets.items():
-        hits, ties = check_hits(scene.intersect(rays), ora.intersect(rays, use_bvh=True), f"{name}/bvh")
+        hits, ties = check_hits(scene.intersect(rays), ora.intersect(rays, use_bvh=True), f"{name}/bvh", rays=rays)
         total += len(rays)
         print(f"{name}: {len(rays)} rays, {hits} hits, {ties} ties")
     assert total >= 1_000_000
@@ -95,8 +95,8 @@ def _check_scene(desc, scene, ora, aspect, lo, hi, n_camera, n_random, n_brute, 
     rng = np.random.default_rng(seed + 1)
     sub = np.concatenate([r[rng.choice(len(r), n_brute // 3, replace=False)] for r in sets.values()])
     brute = ora.intersect(sub, use_bvh=False)
-    check_hits(scene.intersect(sub), brute, "subset/brute")
-    check_hits(ora.intersect(sub, use_bvh=True), brute, "oracle-bvh/brute", min_exact=1.0)
+    check_hits(scene.intersect(sub), brute, "subset/brute", rays=sub)
+    check_hits(ora.intersect(sub, use_bvh=True), brute, "oracle-bvh/brute", min_exact=1.0, rays=sub)
 
 
 def test_intersect_terrain_full_scale(terrain):
