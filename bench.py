@@ -530,7 +530,8 @@ def main():
                                  "these bytes)",
                 "kernel": top,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
-                "avg_launch_ms": per_launch_ms,
+                "avg_launch_ms": per_launch_ms, "algorithmic_bytes_counter_render": alg_bytes,
+                "timed_launches": launches,
                 "nodes_per_ray": st_c["extend_nodes"] / max(st_c["extension_rays"], 1),
                 "tris_per_ray": st_c["extend_tris"] / max(st_c["extension_rays"], 1),
                 "traced_rays_per_launch": rays_k / max(launches, 1),
