@@ -297,8 +297,11 @@ def time_to_1pct(ng, ref_spp=16384, rungs=(256, 1024), w=256, h=256, m=8):
     out = {"workload": f"cornell_box 36 tris, {w}x{h}, pt, max length {m}",
            "reference": {"renderer": "ptdirect", "precision": "fp64", "spp": ref_spp, "seconds": ta + tb,
                          "rel_noise": sigma_ref}}
-    render("pt", "fp32", 16, 3)  # warm both instances
-    render("pt", "fp64", 16, 3)
+    # warm every kernel form the rungs use (a pt render whose samples fit in one wave runs the queued
+    # kernels, a longer one the fused kernel), in both precisions
+    for precision in ("fp32", "fp64"):
+        for spp in rungs:
+            render("pt", precision, spp, 3)
     for precision in ("fp32", "fp64"):
         rs = []
         for spp in rungs:

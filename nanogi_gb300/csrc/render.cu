@@ -1441,7 +1441,9 @@ __global__ void __launch_bounds__(256) k_logic_bdpt(SceneView<R> sv, WaveView<R>
 }
 
 // Which logic kernel a wave runs.
-constexpr int kLogicCamera = 0, kLogicLight = 1, kLogicBdpt = 2;
+// kLogicCameraQ: camera paths with queued (compacted) shading whatever the renderer (pt renders
+// whose samples all fit in one wave)
+constexpr int kLogicCamera = 0, kLogicLight = 1, kLogicBdpt = 2, kLogicCameraQ = 3;
 
 
 // ---- persistent traversal -------------------------------------------------------------------
@@ -2057,7 +2059,7 @@ int trace_grid() {
 // job lookups, and the batch's shadow rays cannot be staged without their job).
 template <bool DIRECT, bool BATCH, int LOGIC>
 constexpr bool compact_shading() {
-    return DIRECT && !BATCH && LOGIC == kLogicCamera;
+    return !BATCH && (LOGIC == kLogicCameraQ || (DIRECT && LOGIC == kLogicCamera));
 }
 
 // Per-iteration counter reset of compacted shading: the queues the iteration fills start empty,
@@ -2152,7 +2154,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     trace_grid<R, STATS, ADJ, BATCH>();
     // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders, batches
     // and the adjoint, outside the measurement renders (which time or count the wavefront kernels)
-    constexpr bool finish = LOGIC == kLogicCamera && !STATS;
+    constexpr bool finish = (LOGIC == kLogicCamera || LOGIC == kLogicCameraQ) && !STATS;
     auto capture = [&](int n) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t e = nullptr;
@@ -2352,13 +2354,18 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     // ramp of its logic launches), which a larger wave spreads over more rays, and its shading
     // visits only queued slots. Terrain, with the wave-end launch: 14.75 ms per 16-spp render at
     // 2^23, 14.36 at 2^25 (every sample in flight at once); 65.5 against 54.9 ms per 64-spp render.
-    // pt, lt and ltdirect keep 2^23: their logic kernel visits every slot of the wave in each
-    // iteration, so a larger wave costs them in the drain (Cornell box, pt: 0.264 s to 1% error at
-    // 2^25 against 0.23 s). bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64):
-    // 2^18. A smaller default for scenes with a small BVH (2^20 below 32 MB) was measured and not
-    // kept: the Cornell box bench ran at 4995 against 4050 Mrays/s, but its convergence study took
-    // 0.253 against 0.225 s and the 256-job batch rendered one job at a time 3719 against 4431 Mrays/s.
-    const bool compacted = p.renderer == NGI_RENDERER_PTDIRECT;
+    // pt runs the same queued kernels when every sample fits in one such wave (Cornell box bench,
+    // 4.2M samples: 6,070 against 4,880 Mrays/s with the fused kernel); longer pt renders keep the
+    // fused kernel and 2^23 slots, which wins in a steady state (the Cornell box's 67M-sample
+    // convergence renders: 0.218 s to 1% error fused at 2^23, 0.250 s queued at 2^25, 0.466 s queued
+    // at 2^23). lt and ltdirect keep 2^23: their logic kernel visits every slot of the wave in each
+    // iteration. bdpt keeps 2 x 32 path vertices per slot (3.8 KB FP32, 6.7 KB FP64): 2^18. A smaller
+    // default for scenes with a small BVH (2^20 below 32 MB) was measured and not kept: the Cornell box
+    // bench ran at 4995 against 4050 Mrays/s, but its convergence study took 0.253 against 0.225 s and
+    // the 256-job batch rendered one job at a time 3719 against 4431 Mrays/s.
+    const bool pt_queued = p.renderer == NGI_RENDERER_PT &&
+                           (p.wave_size > 0 ? (long long)p.wave_size >= p.num_samples : p.num_samples <= (1LL << 25));
+    const bool compacted = p.renderer == NGI_RENDERER_PTDIRECT || pt_queued;
     int Q = p.wave_size > 0 ? p.wave_size : (bdpt ? (1 << 18) : (compacted ? (1 << 25) : (1 << 23)));
     const long long need = std::max<long long>(p.num_samples, 256);
     if ((long long)Q > need) Q = (int)need;
@@ -2398,6 +2405,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
         WaveView<double> v = wv->vd;
         v.film = d_film;
         if (direct) run_wave<double, true, false>(hs, wv, v, rc, ipg, timing, stream);
+        else if (pt_queued) run_wave<double, false, false, false, false, kLogicCameraQ>(hs, wv, v, rc, ipg, timing, stream);
         else run_wave<double, false, false>(hs, wv, v, rc, ipg, timing, stream);
     } else {
         WaveView<float> v = wv->vf;
@@ -2407,6 +2415,7 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
             else run_wave<float, true, false>(hs, wv, v, rc, ipg, timing, stream);
         } else {
             if (counters) run_wave<float, false, true>(hs, wv, v, rc, ipg, timing, stream);
+            else if (pt_queued) run_wave<float, false, false, false, false, kLogicCameraQ>(hs, wv, v, rc, ipg, timing, stream);
             else run_wave<float, false, false>(hs, wv, v, rc, ipg, timing, stream);
         }
     }

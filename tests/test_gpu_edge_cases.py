@@ -121,6 +121,19 @@ def test_launch_shape_does_not_change_the_film(native_lib, cornell, knobs):
     assert np.allclose(other, base, rtol=1e-9, atol=1e-12)
 
 
+def test_pt_fused_and_queued_kernels_render_the_same_film(native_lib, cornell):
+    """pt renders whose samples all fit in one wave run the queued shading and regeneration kernels;
+    a wave smaller than the sample count keeps the fused kernel. Same paths, same film."""
+    desc, path = cornell
+    W, H = 16, 16
+    scene = _scene(path, W / H)
+    kw = dict(renderer="pt", num_samples=W * H * 32, max_num_vertices=8, width=W, height=H, seed=12)
+    queued = _r(**kw).render(scene)
+    fused = _r(wave_size=2048, **kw).render(scene)
+    assert queued.sum() > 0
+    np.testing.assert_allclose(queued, fused, rtol=1e-9, atol=1e-12)
+
+
 def test_empty_and_lightless_scenes(native_lib, tmp_path):
     import nanogi_gb300 as ng
     from nanogi_gb300 import scenegen
