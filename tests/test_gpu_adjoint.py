@@ -182,7 +182,7 @@ def test_torch_autograd_wrapper(inverse_setup):
     with torch.no_grad():
         a2 = (a - 1e-4 * a.grad / a.grad.abs().max()).clamp(0.0, 1.0)
     loss2 = ((Render.apply(a2, e.detach()) - target) ** 2).sum()
-    assert float(loss2) < float(loss)
+    assert float(loss2.detach()) < float(loss.detach())
     scene.set_parameters(ta, te)
 
 
