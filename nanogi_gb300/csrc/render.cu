@@ -170,6 +170,15 @@ struct WaveView {
 // Longest surface-vertex prefix the adjoint carries: paths of up to 17 vertices.
 constexpr int kAdjMaxPrefix = 16;
 
+// A wave's executable graphs, one pair per kind of wave run (an instantiation of run_wave and a graph
+// length). Each render captures its graphs again (the launches take the render's constants by value)
+// and updates the executable graphs in place, which costs far less than instantiating them.
+struct WaveGraphs {
+    const void* kind = nullptr;
+    int iters = 0;
+    cudaGraphExec_t main = nullptr, drain = nullptr;
+};
+
 struct RenderWave {
     int Q = 0;
     int precision = -1;
@@ -181,6 +190,7 @@ struct RenderWave {
     WaveView<float> vf{};
     WaveView<double> vd{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<WaveGraphs> graphs;
 };
 
 // ---- warp helpers ----------------------------------------------------------------------
@@ -1824,6 +1834,10 @@ SceneView<R> make_view(const DeviceScene& ds) {
 
 void free_wave(RenderWave* wv) {
     if (!wv) return;
+    for (WaveGraphs& g : wv->graphs) {
+        if (g.main) cudaGraphExecDestroy(g.main);
+        if (g.drain) cudaGraphExecDestroy(g.drain);
+    }
     for (void* p : wv->bufs) cudaFree(p);
     if (wv->h_ctr) cudaFreeHost(wv->h_ctr);
     if (wv->ev0) cudaEventDestroy(wv->ev0);
@@ -2155,9 +2169,10 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders, batches
     // and the adjoint, outside the measurement renders (which time or count the wavefront kernels)
     constexpr bool finish = (LOGIC == kLogicCamera || LOGIC == kLogicCameraQ) && !STATS;
-    auto capture = [&](int n) {
+    // Captures n iterations into `exec`: an update of the wave's executable graph when it has one
+    // (same launches, this render's arguments), otherwise a new instantiation.
+    auto capture = [&](int n, cudaGraphExec_t& exec_slot) {
         cudaGraph_t graph = nullptr;
-        cudaGraphExec_t e = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < n; it++)
             enqueue_iteration<R, DIRECT, STATS, ADJ, BATCH, LOGIC>(sv, v, rc, wv->ctr, g_logic, g_trace, stream,
@@ -2167,10 +2182,22 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
             if (graph) cudaGraphDestroy(graph);
             throw DeviceError(std::string("graph capture failed: ") + cudaGetErrorString(cap));
         }
-        const cudaError_t inst = cudaGraphInstantiate(&e, graph, 0);
+        if (exec_slot) {
+            cudaGraphExecUpdateResultInfo info{};
+            if (cudaGraphExecUpdate(exec_slot, graph, &info) == cudaSuccess) {
+                cudaGraphDestroy(graph);
+                return;
+            }
+            cudaGetLastError();  // a refused update: instantiate instead
+            cudaGraphExecDestroy(exec_slot);
+            exec_slot = nullptr;
+        }
+        const cudaError_t inst = cudaGraphInstantiate(&exec_slot, graph, 0);
         cudaGraphDestroy(graph);
-        if (inst != cudaSuccess) throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
-        return e;
+        if (inst != cudaSuccess) {
+            exec_slot = nullptr;
+            throw DeviceError(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
+        }
     };
     // Once every sample is claimed, the wave drains: the host then reads the counters after every
     // drain graph (two iterations, one outside compacted shading) so that the wave-end launch starts
@@ -2178,15 +2205,18 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     const int drain_iters = compact ? 2 : 1;
     cudaGraphExec_t exec = nullptr, exec_drain = nullptr;
     if (!kernel_timing) {
-        exec = capture(iters_per_graph);
-        if (finish && drain_iters < iters_per_graph) {
-            try {
-                exec_drain = capture(drain_iters);
-            } catch (...) {
-                cudaGraphExecDestroy(exec);
-                throw;
-            }
+        static const char kind_tag = 0;  // one per instantiation of run_wave
+        WaveGraphs* wg = nullptr;
+        for (WaveGraphs& g : wv->graphs)
+            if (g.kind == &kind_tag && g.iters == iters_per_graph) wg = &g;
+        if (!wg) {
+            wv->graphs.push_back(WaveGraphs{&kind_tag, iters_per_graph, nullptr, nullptr});
+            wg = &wv->graphs.back();
         }
+        capture(iters_per_graph, wg->main);
+        if (finish && drain_iters < iters_per_graph) capture(drain_iters, wg->drain);
+        exec = wg->main;
+        exec_drain = (finish && drain_iters < iters_per_graph) ? wg->drain : nullptr;
     }
     cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
     double kms[2] = {0, 0};
@@ -2261,15 +2291,11 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
         CUDA_CHECK(cudaEventRecord(wv->ev1, stream));
         CUDA_CHECK(cudaEventSynchronize(wv->ev1));
     } catch (...) {
-        cudaStreamSynchronize(stream);
-        if (exec) cudaGraphExecDestroy(exec);
-        if (exec_drain) cudaGraphExecDestroy(exec_drain);
+        cudaStreamSynchronize(stream);  // the wave keeps its graphs
         for (auto& e : kev)
             if (e) cudaEventDestroy(e);
         throw;
     }
-    if (exec) cudaGraphExecDestroy(exec);
-    if (exec_drain) cudaGraphExecDestroy(exec_drain);
     for (auto& e : kev)
         if (e) cudaEventDestroy(e);
     float ms = 0;
