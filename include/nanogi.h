@@ -83,7 +83,8 @@ typedef struct ngi_render_params {
     int64_t sample_offset;     /* first global sample index (sharded / resumed renders) */
     int32_t precision;         /* ngi_precision */
     int32_t raster_mode;       /* ngi_raster_mode */
-    int32_t wave_size;         /* path slots resident on the device; 0 = auto */
+    int32_t wave_size;         /* path slots resident on the device; 0 = auto (2^25 for ptdirect and for pt
+                                  renders of at most 2^25 samples, 2^23 otherwise, never above the samples) */
     int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
     int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
     int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
@@ -200,7 +201,8 @@ NGI_API ngi_status ngi_scene_get_triangles(const ngi_scene* scene, float* pos, f
 NGI_API ngi_status ngi_scene_build(ngi_scene* scene);
 
 /* Frees the render buffers a scene handle keeps between renders (its wave of path slots and
- * queues, up to ~2 GB); the scene itself stays on the device and the next render allocates them
+ * queues: at most 2^25 slots, about 8.6 GB in FP32 and 13.4 GB in FP64, never more slots than a
+ * render's samples); the scene itself stays on the device and the next render allocates them
  * again. For programs that keep many scene handles alive. Not in the reference (its per-thread
  * contexts live for one render, nanogi.cpp:281-319). */
 NGI_API ngi_status ngi_scene_release_buffers(ngi_scene* scene);
