@@ -475,16 +475,20 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
+        # the library runs pt with the queued kernels when the render's samples fit in one wave
+        queued = RENDERER == "ptdirect" or (RENDERER == "pt" and (n_step <= 1 << 25 if args.wave_size == 0
+                                                                  else args.wave_size >= n_step))
         ev0.record(stream)
         for i in range(args.steps):
             flush.zero_()
             st = render_step(base + (args.warmup + i) * n_step)
             totals["rays"] += st["extension_rays"] + st["shadow_rays"]
             totals["samples"] += st["camera_rays"]
-            # ptdirect: counter reset, shading, regeneration and traversal per iteration, plus the
-            # wave's initial carry queue; pt: the fused path logic and traversal; both: the wave-end
-            # launch that runs the last paths to their end
-            totals["launches"] += (4 * st["iterations"] + 1) if RENDERER == "ptdirect" else 2 * st["iterations"]
+            # queued kernels (ptdirect, and pt renders whose samples fit in one wave): counter reset,
+            # shading, regeneration and traversal per iteration, plus the wave's initial regeneration
+            # queue; the fused pt kernel: path logic and traversal; both: the wave-end launch that runs
+            # the last paths to their end
+            totals["launches"] += (4 * st["iterations"] + 1) if queued else 2 * st["iterations"]
             totals["launches"] += 1 if st["finish_paths"] > 0 else 0
         ev1.record(stream)
         torch.cuda.synchronize()
