@@ -475,9 +475,11 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
-        # the library runs pt with the queued kernels when the render's samples fit in one wave
-        queued = RENDERER == "ptdirect" or (RENDERER == "pt" and (n_step <= 1 << 25 if args.wave_size == 0
-                                                                  else args.wave_size >= n_step))
+        # the library runs pt with the queued kernels when the render's samples fit in one wave; a
+        # queued wave that holds every sample runs regeneration in its first iteration only
+        fits = n_step <= 1 << 25 if args.wave_size == 0 else args.wave_size >= n_step
+        queued = RENDERER == "ptdirect" or (RENDERER == "pt" and fits)
+        one_pass = queued and fits
         ev0.record(stream)
         for i in range(args.steps):
             flush.zero_()
@@ -485,10 +487,14 @@ def main():
             totals["rays"] += st["extension_rays"] + st["shadow_rays"]
             totals["samples"] += st["camera_rays"]
             # queued kernels (ptdirect, and pt renders whose samples fit in one wave): counter reset,
-            # shading, regeneration and traversal per iteration, plus the wave's initial regeneration
-            # queue; the fused pt kernel: path logic and traversal; both: the wave-end launch that runs
-            # the last paths to their end
-            totals["launches"] += (4 * st["iterations"] + 1) if queued else 2 * st["iterations"]
+            # shading, regeneration and traversal per iteration (regeneration in the first iteration
+            # only when the wave holds every sample), plus the wave's initial regeneration queue; the
+            # fused pt kernel: path logic and traversal; both: the wave-end launch that runs the last
+            # paths to their end
+            if queued:
+                totals["launches"] += (3 * st["iterations"] + 2) if one_pass else (4 * st["iterations"] + 1)
+            else:
+                totals["launches"] += 2 * st["iterations"]
             totals["launches"] += 1 if st["finish_paths"] > 0 else 0
         ev1.record(stream)
         torch.cuda.synchronize()
