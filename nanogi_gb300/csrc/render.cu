@@ -108,6 +108,7 @@ struct RenderConsts {
     int num_prims;          // primitives of the scene (adjoint gradient layout)
     int ray_offset;         // NGI_RAY_OFFSET_*: absolute tmin = EpsF, or scale-aware origin offsets
     int trace_all;          // NGI_RENDER_TRACE_ALL_RAYS: trace the rays toward hits that cannot score
+    int one_pass;           // the queued wave holds every sample: no regeneration after the first iteration
 };
 
 // One job of a batch render: its scene, parameters, device film and first batch sample.
@@ -812,7 +813,9 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             // queue it comes from, and only the fused kernel reads the array)
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
-            const unsigned mr = __ballot_sync(0xFFFFFFFFu, need_new), me = __ballot_sync(0xFFFFFFFFu, want_ext);
+            // ended paths go to regeneration unless the wave holds every sample (nothing regenerates then)
+            const bool to_regen = need_new && !rc0.one_pass;
+            const unsigned mr = __ballot_sync(0xFFFFFFFFu, to_regen), me = __ballot_sync(0xFFFFFFFFu, want_ext);
             const int warp = (int)(threadIdx.x >> 5);
             if (lane_id() == 0) {
                 s_warp[warp] = __popc(mr);
@@ -837,7 +840,7 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
                 }
             }
             __syncthreads();
-            if (need_new) w.regen_queue[s_base32 + s_warp[warp] + __popc(mr & lanemask_lt())] = s;
+            if (to_regen) w.regen_queue[s_base32 + s_warp[warp] + __popc(mr & lanemask_lt())] = s;
             if (want_ext) w.ext_queue[s_base32b + s_warp2[warp] + __popc(me & lanemask_lt())] = s;
             if constexpr (!ADJ) {
                 const StagedShadow<R>* stage = shadow_stage<R>();
@@ -2151,7 +2154,7 @@ void enqueue_iteration(const SceneView<R>& sv, const WaveView<R>& v, const Rende
 }
 
 template <typename R, bool DIRECT, bool STATS, bool ADJ = false, bool BATCH = false, int LOGIC = 0>
-void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& rc, int iters_per_graph,
+void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, RenderConsts rc, int iters_per_graph,
               bool kernel_timing, cudaStream_t stream, const JobView<R>* jobs = nullptr, int num_jobs = 0) {
     DeviceScene& ds = *hs.dev;
     const SceneView<R> sv = make_view<R>(ds);
@@ -2175,6 +2178,7 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, const RenderConsts& 
     // regeneration kernel could only mark ended slots done, which nothing reads with queued shading,
     // so the later iterations leave it out (terrain: 0.22 ms per 16-spp render).
     const bool one_pass = compact && (long long)v.Q >= rc.num_samples;
+    rc.one_pass = one_pass ? 1 : 0;
     // Captures n iterations into `exec`: an update of the wave's executable graph when it has one
     // (same launches, this render's arguments), otherwise a new instantiation. first: the graph's
     // first iteration may start samples.
