@@ -971,8 +971,11 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
                     block_count_warp(&bc.camera, need_new && st != SLOT_DONE);
                 }
                 need_new = need_new && st == SLOT_EMPTY;
-                if (!__syncthreads_or(need_new)) break;  // block-uniform: the claims are block-wide
+                // block-uniform (the claims are block-wide); a wave that holds every sample has
+                // claimed them all with the first attempts of its slots, so it makes no second one
+                if (!__syncthreads_or(need_new) || rc0.one_pass) break;
             }
+            if (rc0.one_pass && need_new) st = SLOT_DONE;  // its sample ended at the sensor vertex
             if (!want_ext && st == SLOT_ACTIVE) st = SLOT_EMPTY;
             if (want_ext) st = SLOT_ACTIVE;
             if (PART == kLogicFused && valid) w.state[s] = st;  // read only by the fused kernel
