@@ -862,8 +862,12 @@ __global__ void __launch_bounds__(256, PART == kLogicFused    ? kLogicMinBlocks
             // queue). Terrain, ptdirect: 1 attempt 1776, 2 attempts 1833, 3 attempts 1824 Msamples/s.
             for (int attempt = 0; attempt < kRegenAttempts; attempt++) {
                 {
-                    // one atomic per block on the sample counter every slot of the wave claims from
-                    const unsigned long long k = block_claim(&w.ctr->next_sample, need_new, s_warp, &s_base64);
+                    // one atomic per block on the sample counter every slot of the wave claims from; a
+                    // wave that holds every sample gives the slot at queue position i (slot i of the
+                    // identity queue it starts from) sample i instead (block-uniform branch)
+                    const unsigned long long k = rc0.one_pass
+                                                     ? (unsigned long long)item
+                                                     : block_claim(&w.ctr->next_sample, need_new, s_warp, &s_base64);
                     if (need_new) {
                         int job = 0;
                         unsigned long long local = k;
@@ -2101,12 +2105,15 @@ __global__ void k_iteration_begin(WaveCounters* ctr, int parity) {
 // Every slot of a new wave starts empty, in the regeneration queue of the first iteration: its
 // shading launch has no queued slot, and regeneration starts a sample in every slot. (Handing the
 // slots through the carry queue instead took the first shading launch 0.28 ms for 2^25 slots.)
-__global__ void k_wave_init_slots(int* regen_queue, int Q, WaveCounters* ctr) {
+// claimed: the samples the first iteration starts without claiming them (a wave that holds every
+// sample gives slot i sample i), else 0.
+__global__ void k_wave_init_slots(int* regen_queue, int Q, WaveCounters* ctr, unsigned long long claimed) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < Q) regen_queue[i] = i;
     if (i == 0) {
         ctr->regen_seed = Q;
         ctr->carry_count[0] = 0;
+        ctr->next_sample = claimed;
     }
 }
 
@@ -2167,8 +2174,15 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, RenderConsts rc, int
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(wv->ctr, 0, sizeof(WaveCounters), stream));
     constexpr bool compact = compact_shading<DIRECT, BATCH, LOGIC>();
+    // A queued wave that holds every sample starts them all in its first iteration, slot i with
+    // sample i (no claims on the sample counter); after it, the regeneration kernel could only mark
+    // ended slots done, which nothing reads with queued shading, so the later iterations leave it out
+    // (terrain: 0.22 ms per 16-spp render).
+    const bool one_pass = compact && (long long)v.Q >= rc.num_samples;
+    rc.one_pass = one_pass ? 1 : 0;
     if constexpr (compact) {
-        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, wv->ctr);
+        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, wv->ctr,
+                                                                  one_pass ? (unsigned long long)v.Q : 0ull);
         CUDA_CHECK(cudaGetLastError());
         iters_per_graph += iters_per_graph & 1;  // queue parity must restart at 0 with every graph launch
     }
@@ -2177,11 +2191,6 @@ void run_wave(HostScene& hs, RenderWave* wv, WaveView<R> v, RenderConsts rc, int
     // the wave's end in one launch (k_finish): pt and ptdirect camera paths, single renders, batches
     // and the adjoint, outside the measurement renders (which time or count the wavefront kernels)
     constexpr bool finish = (LOGIC == kLogicCamera || LOGIC == kLogicCameraQ) && !STATS;
-    // A queued wave that holds every sample starts them all in its first iteration; after it, the
-    // regeneration kernel could only mark ended slots done, which nothing reads with queued shading,
-    // so the later iterations leave it out (terrain: 0.22 ms per 16-spp render).
-    const bool one_pass = compact && (long long)v.Q >= rc.num_samples;
-    rc.one_pass = one_pass ? 1 : 0;
     // Captures n iterations into `exec`: an update of the wave's executable graph when it has one
     // (same launches, this render's arguments), otherwise a new instantiation. first: the graph's
     // first iteration may start samples.
@@ -2977,7 +2986,7 @@ void run_wave_noalloc(HostScene& hs, WaveView<R> v, const RenderConsts& rc, int 
     CUDA_CHECK(cudaMemsetAsync(v.state, SLOT_EMPTY, (size_t)v.Q, stream));
     CUDA_CHECK(cudaMemsetAsync(v.ctr, 0, sizeof(WaveCounters), stream));
     if constexpr (compact_shading<DIRECT, false, kLogicCamera>())
-        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, v.ctr);
+        k_wave_init_slots<<<(v.Q + 255) / 256, 256, 0, stream>>>(v.regen_queue, v.Q, v.ctr, 0ull);
     const long long per_slot = (long long)((rc.num_samples + v.Q - 1) / v.Q) + 1;
     const long long max_iters = per_slot * (long long)(rc.max_vertices > 0 ? rc.max_vertices + 2 : 4096) + 64;
     WaveCounters h{};
