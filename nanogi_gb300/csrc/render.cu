@@ -2048,7 +2048,7 @@ int grid_for(int items, int block) {
 
 // Blocks of a persistent kernel that fit on the device at once. Measured and not kept: a preferred
 // shared-memory carve-out of 0 (the largest L1) for the traversal (1768 against 1809 Mrays/s on
-// the terrain with the driver's choice) or for the path logic (1810: no change).
+// the terrain with the CUDA driver's default) or for the path logic (1810: no change).
 template <typename K>
 int persistent_grid(K kernel, int block) {
     int dev = 0, sms = 152, per_sm = 1;
