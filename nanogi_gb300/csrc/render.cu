@@ -1604,7 +1604,10 @@ constexpr int kFinishMaxVertices = 4096;
 // Paths left in flight below which the wave hands them to k_finish: its time grows with the paths it
 // gets (the longest of them sets it), while one more drain iteration costs a full set of launches.
 // Terrain, ptdirect, 2^25-slot wave: 8192 paths 14.59 ms per 16-spp render, 32768 14.43, 131072
-// 14.36; per 64-spp render 55.33, 55.10 and 54.89 ms.
+// 14.36; per 64-spp render 55.33, 55.10 and 54.89 ms. Later kernels, 131072 against larger limits:
+// the terrain keeps 292,617 paths after four iterations, so 262144 is the same (12.73 ms) and 524288
+// finishes all of them at once (13.26 ms); the interior (1024^2, max length 32) 15.23 against 15.61
+// (262144) and 15.67 ms (524288).
 constexpr int kFinishMaxPaths = 131072;
 template <typename R, bool DIRECT, bool BATCH, bool ADJ>
 __global__ void __launch_bounds__(kFinishBlock)
