@@ -86,7 +86,8 @@ typedef struct ngi_render_params {
     int32_t wave_size;         /* path slots resident on the device; 0 = auto (2^25 for ptdirect and for pt
                                   renders of at most 2^25 samples, 2^18 for bdpt, 2^23 otherwise, never above
                                   the samples) */
-    int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto */
+    int32_t iterations_per_graph; /* wave iterations per CUDA-graph launch; 0 = auto (6 for a ptdirect
+                                     or pt wave that holds every sample, else 4) */
     int32_t flags;             /* NGI_RENDER_* measurement flags, 0 for normal renders */
     int32_t trace_refill;      /* idle lanes that make a traversal warp fetch new rays (1..32); 0 = auto */
     int32_t reserved;          /* must be 0 */

@@ -2429,7 +2429,14 @@ void DeviceRender(HostScene& hs, const ngi_render_params& p, double* d_film, cud
     Q = (Q + 255) / 256 * 256;
     RenderWave* wv = ensure_wave(ds, Q, p.precision);
     const RenderConsts rc = consts_of(p, (int)hs.prims.size());
-    const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : 4;
+    // Wave iterations between two reads of the counters. A compacted wave that holds every sample
+    // runs 6 in its first graph, after which the terrain is below the wave end's threshold without a
+    // drain graph and its host round trip: 12.85 against 12.89 ms per 16-spp render, Cornell box bench
+    // 7,060 against 6,999 Mrays/s, interior 15.31 against 15.33 ms per 16-spp render. 8 was slower on
+    // the terrain (13.07 ms: two more wavefront iterations instead of the wave-end launch). Other
+    // waves run 4.
+    const bool holds_all = compacted && (long long)wv->Q >= p.num_samples;
+    const int ipg = p.iterations_per_graph > 0 ? p.iterations_per_graph : (holds_all ? 6 : 4);
     const bool timing = (p.flags & NGI_RENDER_KERNEL_TIMING) != 0;
     const bool counters = (p.flags & NGI_RENDER_TRAVERSAL_COUNTERS) != 0;
     const bool direct = p.renderer == NGI_RENDERER_PTDIRECT || p.renderer == NGI_RENDERER_LTDIRECT;
